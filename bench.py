@@ -1,0 +1,342 @@
+"""Benchmark of the particle step: particle-steps/s on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload box512_clustered] [--form fp64|fp32]
+
+A step is one RK4 step (4 stages + the per-step reorder) of every particle:
+interpolation, advance, wrap, and the concentration, momentum and energy
+deposits. Inputs are seeded synthetic fields and particles of the workload's
+shapes (first_repo_gb300/csrc/pstep_gen.c); no dataset is involved.
+
+value  : particle-steps/s with everything resident in HBM (CUDA events around
+         K steps on the library's stream), summed over ranks.
+e2e    : the same metric through the C ABI with host buffers: per step the
+         particle state and gas fields are copied in from pinned host memory and
+         the particle state and the deposited fields copied back.
+roofline: the dominant kernel phase, algorithmic bytes per launch / its mean
+         launch time (CUDA events around the phase during the timed region).
+cpu_baseline: the oracle (C restatement of the reference step, single thread as
+         the reference runs per rank) on a bounded sample of the workload.
+--impl reference: the reference's CPU step (the oracle port; the reference's own
+         build needs its sources, which exist only where it was compiled) on
+         all host cores, one independent single-rank instance per core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from first_repo_gb300 import config, gen  # noqa: E402
+
+# Algorithmic (compulsory) bytes, FP64 drop-in form, per particle per stage of
+# each phase, and per ghosted cell per launch. Keep in step with the kernels.
+#   advance  k=0 reads base(7) + RHS_T + x_int record (3 frac + key) = 92 B,
+#            writes new(7) + np1(7) + new record(3 frac + key) + RHS_T + RHS_u(3) + leave code = 173 B;
+#            k=1..3 also read *_int(7) and *_np1(7) = +112 B;  fields U(3) and T read once per launch.
+FP64_ADVANCE_BYTES = {0: 92 + 173, 1: 92 + 173 + 112, 2: 92 + 173 + 112, 3: 92 + 173 + 112}
+FP64_ADVANCE_CELL_BYTES = 4 * 8
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for nm, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM, "fallback"
+
+
+def make_inputs(wl, dp_over_dx=0.1, mass_loading=0.2):
+    t0 = time.time()
+    case = gen.make_case(wl.n, wl.n_particles, wl.seed, wl.clustered)
+    bp = config.box_params(wl.n, wl.n_particles, dp_over_dx=dp_over_dx, mass_loading=mass_loading)
+    fields = [gen.ghost(case[k]) for k in ("ux", "uy", "uz", "T")]
+    return case, bp, fields, time.time() - t0
+
+
+def pinned_like(a: np.ndarray) -> np.ndarray:
+    import torch
+    t = torch.empty(a.shape, dtype=torch.float64 if a.dtype == np.float64 else torch.int32, pin_memory=True)
+    out = t.numpy()
+    out[...] = a
+    out._torch_ref = t  # noqa: keep the pinned allocation alive
+    return out
+
+
+def cpu_sample_rate(n_cells=160, count=1 << 22, steps=2, seed=77, clustered=True):
+    """Oracle (single thread) on a bounded sample with the workload's density and construction."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    case = gen.make_case(n_cells, count, seed, clustered)
+    bp = config.box_params(n_cells, count)
+    o = pyoracle.Oracle(bp.step_config(), count)
+    o.load(case["x"], case["y"], case["z"], case["u"], case["v"], case["w"], case["t"], case["flag"])
+    ux, uy, uz, tf = (gen.ghost(case[k]) for k in ("ux", "uy", "uz", "T"))
+    o.prime(tf)
+    t0 = time.perf_counter()
+    o.run(steps, ux, uy, uz, tf)
+    dt = time.perf_counter() - t0
+    return count * steps / dt, dt
+
+
+def _ref_worker(args):
+    n_cells, count, steps, seed = args
+    rate, dt = cpu_sample_rate(n_cells, count, steps, seed)
+    return rate, dt
+
+
+def run_reference(args, wl):
+    rank, _, world = rank_info()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    n_cells, count = 128, 1 << 21
+    ctx = mp.get_context("spawn")
+    rates = []
+    t_all = []
+    # warm-up: one step on one core (builds nothing new; page-in of the library)
+    for _ in range(max(1, args.warmup // 3)):
+        cpu_sample_rate(32, 1 << 15, 1)
+    with ctx.Pool(cores) as pool:
+        for s in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_ref_worker, [(n_cells, count, 1, 1000 + 7 * i + s) for i in range(cores)])
+            wall = time.perf_counter() - t0
+            slowest = max(r[1] for r in res)
+            rates.append(cores * count / slowest)
+            t_all.append(wall)
+    value = float(np.median(rates))
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wl.n_particles / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": wl.name, "cells": wl.n ** 3, "particles": wl.n_particles,
+                   "sample": f"{cores} independent single-rank instances x {count} particles on {n_cells}^3 "
+                             "(the workload's particle density and construction), 1 step each"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} x {count} particles on {n_cells}^3, 1 RK4 step"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="box512_clustered", choices=sorted(config.WORKLOADS))
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    wl = config.WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+        return
+
+    rank, local, world = rank_info()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    from first_repo_gb300 import pstep
+    case, bp, fields, gen_s = make_inputs(wl)
+    form = pstep.FP32 if args.form == "fp32" else pstep.FP64
+    flags = pstep.TRACK_ORDER if form == pstep.FP64 else 0
+    n = wl.n_particles
+    arrs = [np.ascontiguousarray(case[k]) for k in ("x", "y", "z", "u", "v", "w", "t", "flag")]
+    g = pstep.ParticleStep(bp.step_config(), n, form, flags)
+    g.load(*arrs)
+    g.bind_velocity(*fields[:3])
+    g.bind_temperature(fields[3])
+    g.prime()
+    for _ in range(args.warmup):
+        g.run(1)
+    rc, wflags = g.check()
+    if rc != 0:
+        raise SystemExit(f"device check failed after warm-up: {wflags}")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    clocks = Clocks(local)
+    g.profile(True)
+    g.profile_read()
+    l0 = g.launches()
+    clocks.start()
+    barrier()
+    g.run(args.steps)
+    ms = g.last_run_ms()
+    barrier()
+    clocks.stop()
+    launches = g.launches() - l0
+    prof = g.profile_read()
+    g.profile(False)
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * n / (ms_per_step / 1e3)
+
+    # roofline of the dominant phase
+    peak, peak_kind = peaks()
+    dom = max(prof, key=lambda p: prof[p][0])
+    dom_ms, dom_cnt = prof[dom]
+    roof = None
+    if dom == "advance" and dom_cnt:
+        per_launch = n * sum(FP64_ADVANCE_BYTES.values()) / 4.0 + FP64_ADVANCE_CELL_BYTES * (wl.n + 2) ** 3
+        achieved = per_launch / (dom_ms / dom_cnt / 1e3) / 1e9
+        traffic = None
+        tf_path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+        if os.path.exists(tf_path):
+            with open(tf_path) as f:
+                traffic = json.load(f).get(f"{args.form}_advance_{wl.name}")
+        roof = {"kernel": "k_advance", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": per_launch, "mean_launch_ms": dom_ms / dom_cnt}
+    phases = {p: {"ms_per_step": v[0] / args.steps, "launch_groups": v[1]} for p, v in prof.items()}
+
+    # end to end through the C ABI with host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        hp = [pinned_like(a) for a in arrs]
+        hf = [pinned_like(f) for f in fields]
+        out_p = [pinned_like(np.empty(n)) for _ in range(7)]
+        out_f = [pinned_like(np.empty_like(fields[0])) for _ in range(5)]
+        names = ["x", "y", "z", "u", "v", "w", "T"]
+        import ctypes as C
+        L = pstep.lib()
+
+        def one_step():
+            g.load(*hp)
+            g.bind_velocity(*hf[:3])
+            g.bind_temperature(hf[3])
+            g.prime()
+            g.run(1)
+            for i, nm in enumerate(names):
+                g._ok(L.pstep_get_particle_array(g.h, pstep.ARRAY_IDS[nm], out_p[i].ctypes.data, 0))
+            for i, fname in enumerate(pstep.FIELD_IDS):
+                g._ok(L.pstep_get_field(g.h, pstep.FIELD_IDS[fname], out_f[i].ctypes.data, 0))
+
+        one_step()
+        barrier()
+        t0 = time.perf_counter()
+        ke = max(1, args.steps)
+        for _ in range(ke):
+            one_step()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / ke
+        h2d = sum(a.nbytes for a in hp) + sum(f.nbytes for f in hf)
+        d2h = sum(a.nbytes for a in out_p) + sum(f.nbytes for f in out_f)
+        e2e = {"value": world * n / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3}
+        del C
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, dt = cpu_sample_rate()
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": f"{1 << 22} particles on 160^3 (the workload's density and construction), 2 RK4 steps, "
+                         f"{dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == pstep.FP64 else "f32",
+            "data": "synthetic",
+            "config": {"workload": wl.name, "cells": wl.n ** 3, "particles": n, "form": args.form,
+                       "order_tracking": bool(flags & pstep.TRACK_ORDER), "clustered": wl.clustered,
+                       "l2": "inputs larger than L2 (particle state alone is several GB)",
+                       "parallelism": f"replicas x{world}", "input_generation_s": round(gen_s, 2)},
+            "roofline": roof, "phases": phases, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -84,7 +84,7 @@ def build_cuda(force: bool = False, verbose_ptxas: bool = False) -> str:
         obj = os.path.join(OUT, u.replace(".cu", ".o"))
         objs.append(obj)
         if force or not _newer(obj, [src] + hdrs):
-            cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                    "-I", INCLUDE, "-I", CSRC, *CU_UNITS[u], "-c", src, "-o", obj]
             if verbose_ptxas:
                 cmd.insert(1, "-Xptxas=-v")

@@ -1,0 +1,348 @@
+// Two-way-coupling deposition, FP64 drop-in form, as target-cell gathers.
+//
+// Each thread owns one target cell of the ghosted grid and walks the sorted
+// particles (CSR by node key) of the few nodes whose stencils reach it, merging
+// the node lists by the CSR's secondary key. With PSTEP_TRACK_ORDER that key is
+// the particle's position in the reference's vectors, so every cell receives
+// its contributions in exactly the order the reference's scatter loop adds them
+// (particle.cpp:498-658), from 0, with the reference's weight expressions; the
+// cumulative ghost fold and the ghost refresh then replay communicator.cpp's
+// single-rank sequence. No atomics: the result is the same on every run.
+//
+// Compiled with -fmad=false (see stage_f64.cu).
+#include "pstep_internal.cuh"
+
+namespace pstep {
+namespace {
+
+struct DepIn {
+  const int32_t *cell_start;  // gsize + 1
+  const int32_t *sidx;        // nullptr: identity
+  const int32_t *order;       // secondary key per particle (nullptr: storage index)
+  const double *frac[3];
+  const uint32_t *key;
+  const double *val[3];       // RHS_u,v,w (int-deposit) or RHS_T in val[0] (temperature deposit)
+};
+
+__device__ inline int32_t pidx(const DepIn &d, int32_t p) { return d.sidx ? d.sidx[p] : p; }
+__device__ inline int32_t okey(const DepIn &d, int32_t q) { return d.order ? d.order[q] : q; }
+
+// K-way merge over node segments, calling f(particle) in ascending secondary-key order.
+template <int K, typename F>
+__device__ inline void merge_walk(const DepIn &d, const long long (&nodes)[K], F f) {
+  int32_t cur[K], end[K], head[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    if (nodes[q] >= 0) {
+      cur[q] = d.cell_start[nodes[q]];
+      end[q] = d.cell_start[nodes[q] + 1];
+    } else {
+      cur[q] = 0;
+      end[q] = 0;
+    }
+    head[q] = cur[q] < end[q] ? okey(d, pidx(d, cur[q])) : INT32_MAX;
+  }
+  while (true) {
+    int best = -1;
+    int32_t bk = INT32_MAX;
+#pragma unroll
+    for (int q = 0; q < K; ++q)
+      if (head[q] < bk) { bk = head[q]; best = q; }
+    if (best < 0) break;
+#pragma unroll
+    for (int q = 0; q < K; ++q)
+      if (q == best) {
+        f(pidx(d, cur[q]), q);
+        ++cur[q];
+        head[q] = cur[q] < end[q] ? okey(d, pidx(d, cur[q])) : INT32_MAX;
+      }
+  }
+}
+
+__device__ inline bool node_ok(const Geom &G, int i, int j, int k) {
+  // particle nodes are round(x*idx)+1 in 1..n+1
+  return i >= 1 && i <= G.n[0] + 1 && j >= 1 && j <= G.n[1] + 1 && k >= 1 && k <= G.n[2] + 1;
+}
+
+__device__ inline double xl_round(double f, int h) { return (h ? (f - 1.0) : f) + 0.5; }
+
+// Trilinear deposit (concentration weights, or weights * RHS_T) into target t:
+// contributions come from nodes t + {0,1}^3; offset o = node - t selects the
+// factor (o ? 1 - x_l : x_l) per dimension, combined as ((fx*fy)*fz)[*val] --
+// the operand order of every term in particle.cpp:548-555 and :645-652.
+__global__ void k_dep_trilinear(Geom G, DepIn d, int with_val, double *__restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= G.gsize) return;
+  const int ti = (int)(t % G.g[0]);
+  const int tj = (int)((t / G.g[0]) % G.g[1]);
+  const int tk = (int)(t / ((long long)G.g[0] * G.g[1]));
+  long long nodes[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    int ox = (q >> 2) & 1, oy = (q >> 1) & 1, oz = q & 1;
+    int ni = ti + ox, nj = tj + oy, nk = tk + oz;
+    nodes[q] = node_ok(G, ni, nj, nk) ? glin(G, ni, nj, nk) : -1;
+  }
+  double acc = 0.0;
+  merge_walk<8>(d, nodes, [&](int32_t p, int q) {
+    const uint32_t key = d.key[p];
+    const int ox = (q >> 2) & 1, oy = (q >> 1) & 1, oz = q & 1;
+    const double xl = xl_round(d.frac[0][p], (key >> 2) & 1);
+    const double yl = xl_round(d.frac[1][p], (key >> 1) & 1);
+    const double zl = xl_round(d.frac[2][p], key & 1);
+    const double fx = ox ? (1 - xl) : xl;
+    const double fy = oy ? (1 - yl) : yl;
+    const double fz = oz ? (1 - zl) : zl;
+    double w = fx * fy * fz;
+    if (with_val) w = w * d.val[0][p];
+    acc += w;
+  });
+  out[t] = acc;
+}
+
+// Face-normal momentum deposit (particle.cpp:498-524): x-face t receives
+// x_l*RHS_u from particles whose trunc cell (ghosted) is (ti-1, tj, tk) and
+// (1-x_l)*RHS_u from those in (ti, tj, tk); trunc cell = node - h.
+template <int D>
+__global__ void k_dep_face(Geom G, DepIn d, double *__restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= G.gsize) return;
+  const int tc[3] = {(int)(t % G.g[0]), (int)((t / G.g[0]) % G.g[1]), (int)(t / ((long long)G.g[0] * G.g[1]))};
+  // nodes: along D in {t-1, t, t+1}, across in {t, t+1}
+  long long nodes[12];
+#pragma unroll
+  for (int q = 0; q < 12; ++q) {
+    int a = q / 4 - 1, b = (q >> 1) & 1, c = q & 1;
+    int n3[3];
+    n3[D] = tc[D] + a;
+    n3[(D + 1) % 3] = tc[(D + 1) % 3] + b;
+    n3[(D + 2) % 3] = tc[(D + 2) % 3] + c;
+    nodes[q] = node_ok(G, n3[0], n3[1], n3[2]) ? glin(G, n3[0], n3[1], n3[2]) : -1;
+  }
+  double acc = 0.0;
+  merge_walk<12>(d, nodes, [&](int32_t p, int q) {
+    const uint32_t key = d.key[p];
+    const long long lin = key >> 3;
+    const int h3[3] = {(int)((key >> 2) & 1), (int)((key >> 1) & 1), (int)(key & 1)};
+    const int n3[3] = {(int)(lin % G.g[0]), (int)((lin / G.g[0]) % G.g[1]),
+                       (int)(lin / ((long long)G.g[0] * G.g[1]))};
+    const int c0 = n3[D] - h3[D];
+    const int c1 = n3[(D + 1) % 3] - h3[(D + 1) % 3];
+    const int c2 = n3[(D + 2) % 3] - h3[(D + 2) % 3];
+    if (c1 != tc[(D + 1) % 3] || c2 != tc[(D + 2) % 3]) return;
+    const double xl = d.frac[D][p];
+    if (c0 == tc[D] - 1) acc += xl * d.val[D][p];
+    else if (c0 == tc[D]) acc += (1 - xl) * d.val[D][p];
+  });
+  out[t] = acc;
+}
+
+// communicator.cpp:422-511 on one rank, one phase per launch; nf fields at once
+struct FieldSet {
+  double *f[5];
+  int nf;
+};
+
+__global__ void k_fold_z(Geom G, FieldSet fs) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long plane = (long long)G.g[0] * G.g[1];
+  if (t >= plane * fs.nf) return;
+  int q = (int)(t / plane);
+  long long ij = t % plane;
+  double *f = fs.f[q];
+  const int K = G.g[2];
+  double top = f[(long long)(K - 1) * plane + ij], bot = f[ij];
+  f[(long long)(K - 2) * plane + ij] += bot;
+  f[plane + ij] += top;
+}
+
+__global__ void k_fold_y(Geom G, FieldSet fs) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long per = (long long)G.g[0] * G.n[2];
+  if (t >= per * fs.nf) return;
+  int q = (int)(t / per);
+  long long r = t % per;
+  int i = (int)(r % G.g[0]), k = (int)(r / G.g[0]) + 1;
+  double *f = fs.f[q];
+  const int J = G.g[1];
+  double top = f[glin(G, i, J - 1, k)], bot = f[glin(G, i, 0, k)];
+  f[glin(G, i, J - 2, k)] += bot;
+  f[glin(G, i, 1, k)] += top;
+}
+
+__global__ void k_fold_x(Geom G, FieldSet fs) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long per = (long long)G.n[1] * G.n[2];
+  if (t >= per * fs.nf) return;
+  int q = (int)(t / per);
+  long long r = t % per;
+  int j = (int)(r % G.n[1]) + 1, k = (int)(r / G.n[1]) + 1;
+  double *f = fs.f[q];
+  const int I = G.g[0];
+  double top = f[glin(G, I - 1, j, k)], bot = f[glin(G, 0, j, k)];
+  f[glin(G, I - 2, j, k)] += bot;
+  f[glin(G, 1, j, k)] += top;
+}
+
+// communicator.cpp:177-278 on one rank: x (interior j,k), y (all i, interior k), z (all i,j)
+__global__ void k_refresh_x(Geom G, FieldSet fs) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long per = (long long)G.n[1] * G.n[2];
+  if (t >= per * fs.nf) return;
+  int q = (int)(t / per);
+  long long r = t % per;
+  int j = (int)(r % G.n[1]) + 1, k = (int)(r / G.n[1]) + 1;
+  double *f = fs.f[q];
+  const int I = G.g[0];
+  f[glin(G, I - 1, j, k)] = f[glin(G, 1, j, k)];
+  f[glin(G, 0, j, k)] = f[glin(G, I - 2, j, k)];
+}
+
+__global__ void k_refresh_y(Geom G, FieldSet fs) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long per = (long long)G.g[0] * G.n[2];
+  if (t >= per * fs.nf) return;
+  int q = (int)(t / per);
+  long long r = t % per;
+  int i = (int)(r % G.g[0]), k = (int)(r / G.g[0]) + 1;
+  double *f = fs.f[q];
+  const int J = G.g[1];
+  f[glin(G, i, J - 1, k)] = f[glin(G, i, 1, k)];
+  f[glin(G, i, 0, k)] = f[glin(G, i, J - 2, k)];
+}
+
+__global__ void k_refresh_z(Geom G, FieldSet fs) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long plane = (long long)G.g[0] * G.g[1];
+  if (t >= plane * fs.nf) return;
+  int q = (int)(t / plane);
+  long long ij = t % plane;
+  double *f = fs.f[q];
+  const int K = G.g[2];
+  f[(long long)(K - 1) * plane + ij] = f[plane + ij];
+  f[ij] = f[(long long)(K - 2) * plane + ij];
+}
+
+// Interior sum, fixed order: per-block tree over a strided range, then one block.
+constexpr int kRedBlocks = 1024;
+__global__ void k_sum_partial(Geom G, const double *__restrict__ f, double *__restrict__ part) {
+  __shared__ double sm[kThreads];
+  const long long n3 = (long long)G.n[0] * G.n[1] * G.n[2];
+  double s = 0.0;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n3; c += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(c % G.n[0]) + 1, j = (int)((c / G.n[0]) % G.n[1]) + 1, k = (int)(c / ((long long)G.n[0] * G.n[1])) + 1;
+    s += f[glin(G, i, j, k)];
+  }
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = kThreads / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+__global__ void k_sum_final(const double *__restrict__ part, int np, double inv_count, double *__restrict__ out) {
+  __shared__ double sm[kThreads];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += kThreads) s += part[i];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = kThreads / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sm[0] * inv_count;
+}
+
+inline int blocks_for(long long n) { return (int)((n + kThreads - 1) / kThreads); }
+
+DepIn make_in(pstep_ctx *h, const Csr &csr, double *const frac[3], const uint32_t *key, const double *v0,
+              const double *v1, const double *v2) {
+  DepIn d;
+  d.cell_start = csr.cell_start;
+  d.sidx = csr.identity ? nullptr : csr.sidx;
+  d.order = (h->cfg.flags & PSTEP_TRACK_ORDER) ? h->ref_of_phys : nullptr;
+  for (int q = 0; q < 3; ++q) d.frac[q] = frac[q];
+  d.key = key;
+  d.val[0] = v0;
+  d.val[1] = v1;
+  d.val[2] = v2;
+  return d;
+}
+
+}  // namespace
+
+int fold_fields(pstep_ctx *h, double *const *f, int nf, int refresh) {
+  const Geom &G = h->geom;
+  FieldSet fs;
+  fs.nf = nf;
+  for (int q = 0; q < nf; ++q) fs.f[q] = f[q];
+  long long plane = (long long)G.g[0] * G.g[1];
+  k_fold_z<<<blocks_for(plane * nf), kThreads, 0, h->stream>>>(G, fs);
+  PSTEP_LAUNCHED(h);
+  k_fold_y<<<blocks_for((long long)G.g[0] * G.n[2] * nf), kThreads, 0, h->stream>>>(G, fs);
+  PSTEP_LAUNCHED(h);
+  k_fold_x<<<blocks_for((long long)G.n[1] * G.n[2] * nf), kThreads, 0, h->stream>>>(G, fs);
+  PSTEP_LAUNCHED(h);
+  if (refresh) {
+    k_refresh_x<<<blocks_for((long long)G.n[1] * G.n[2] * nf), kThreads, 0, h->stream>>>(G, fs);
+    PSTEP_LAUNCHED(h);
+    k_refresh_y<<<blocks_for((long long)G.g[0] * G.n[2] * nf), kThreads, 0, h->stream>>>(G, fs);
+    PSTEP_LAUNCHED(h);
+    k_refresh_z<<<blocks_for(plane * nf), kThreads, 0, h->stream>>>(G, fs);
+    PSTEP_LAUNCHED(h);
+  }
+  return PSTEP_OK;
+}
+
+int interior_mean(pstep_ctx *h, const double *f, double *out_dev) {
+  const Geom &G = h->geom;
+  k_sum_partial<<<kRedBlocks, kThreads, 0, h->stream>>>(G, f, h->red_partials);
+  PSTEP_LAUNCHED(h);
+  double inv = 1.0 / (double)((long long)G.n[0] * G.n[1] * G.n[2]);
+  k_sum_final<<<1, kThreads, 0, h->stream>>>(h->red_partials, kRedBlocks, inv, out_dev);
+  PSTEP_LAUNCHED(h);
+  return PSTEP_OK;
+}
+
+// part2gas_Temp_int/new: deposit RHS_T with the records of csr/frac/key, fold, refresh, mean.
+int deposit_temperature(pstep_ctx *h, const Csr &csr, double *const frac[3], const uint32_t *key) {
+  const Geom &G = h->geom;
+  DepIn d = make_in(h, csr, frac, key, h->s.rhs_t, nullptr, nullptr);
+  double *out = h->dep[PSTEP_FIELD_PART_TEMP];
+  k_dep_trilinear<<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, 1, out);
+  PSTEP_LAUNCHED(h);
+  double *fl[1] = {out};
+  int rc = fold_fields(h, fl, 1, 1);
+  if (rc) return rc;
+  return interior_mean(h, out, h->emean_dev);
+}
+
+// part2gas_concentration + part2gas_velocity at x_int (records of the previous CSR)
+int f64_deposit_int(pstep_ctx *h) {
+  const Geom &G = h->geom;
+  DepIn d = make_in(h, h->csr_prev, h->s.frac_prev, h->s.key_prev, h->s.rhs_u[0], h->s.rhs_u[1], h->s.rhs_u[2]);
+  k_dep_trilinear<<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, 0, h->dep[PSTEP_FIELD_C]);
+  PSTEP_LAUNCHED(h);
+  double *c1[1] = {h->dep[PSTEP_FIELD_C]};
+  int rc = fold_fields(h, c1, 1, 0);  // the reference does not refresh C's ghosts
+  if (rc) return rc;
+  if (h->cfg.twc) {
+    k_dep_face<0><<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, h->dep[PSTEP_FIELD_RU_X]);
+    PSTEP_LAUNCHED(h);
+    k_dep_face<1><<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, h->dep[PSTEP_FIELD_RU_Y]);
+    PSTEP_LAUNCHED(h);
+    k_dep_face<2><<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, h->dep[PSTEP_FIELD_RU_Z]);
+    PSTEP_LAUNCHED(h);
+    double *ru[3] = {h->dep[PSTEP_FIELD_RU_X], h->dep[PSTEP_FIELD_RU_Y], h->dep[PSTEP_FIELD_RU_Z]};
+    rc = fold_fields(h, ru, 3, 1);
+    if (rc) return rc;
+  } else {
+    for (int q = PSTEP_FIELD_RU_X; q <= PSTEP_FIELD_RU_Z; ++q)
+      PSTEP_CUDA(cudaMemsetAsync(h->dep[q], 0, sizeof(double) * G.gsize, h->stream));  // RHS_RU = 0 (grid.cpp:671)
+  }
+  return PSTEP_OK;
+}
+
+}  // namespace pstep

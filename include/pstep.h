@@ -1,0 +1,200 @@
+/*
+ * pstep.h -- C ABI of the GB300 (sm_103a) Lagrangian particle step.
+ *
+ * A drop-in for the particle stage of the reference solver (ggeraci/first_repo):
+ * the reference's `class particle` (particle.h:12-155) keeps its call surface in
+ * a replacement particle.cpp that forwards to these entry points, and gas fields
+ * keep the reference's ghosted tensor layout (tensor0.cpp:72-80):
+ *
+ *     field[(k*(ny+2) + j)*(nx+2) + i],  local index = global index + 1 (bs = 1)
+ *
+ * with u.x on the left x-face of cell i, u.y on the lower y-face, u.z on the
+ * lower z-face and T at cell centres (particle.cpp:346-355, :409-415).
+ *
+ * Conventions:
+ *  - every entry point returns a pstep_status (0 = PSTEP_OK); nothing traps;
+ *  - pointers are plain host or device pointers, sizes are element counts;
+ *    `on_device` says which (1 = device pointer on the handle's device);
+ *  - work is enqueued on the handle's stream (pstep_set_stream); calls that
+ *    return data to host memory synchronise that stream;
+ *  - one handle = one device = one rank's particles; the reference's MPI
+ *    migration is replaced by periodic wrap on the single GPU.
+ *
+ * Precisions:
+ *  - PSTEP_FP64: the plain drop-in. Particle states, cell indices, the wrap and
+ *    the particle order (the permutation that Send_Recv, particle.cpp:745-858,
+ *    leaves behind) are bit-identical to the reference; deposited fields match
+ *    it to round-off of a different (fixed, deterministic) summation order.
+ *  - PSTEP_FP32: mixed form. Positions as int32 cell + fp32 offset, fields and
+ *    ODE arithmetic in fp32; deposits accumulated in fp64-class precision and
+ *    written as fp64; balance reductions in fp64.
+ */
+#ifndef PSTEP_H
+#define PSTEP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pstep_ctx *pstep_handle;
+
+typedef enum {
+  PSTEP_OK = 0,
+  PSTEP_ERR_ARG = 1,        /* null handle/pointer, bad id, bad stage index */
+  PSTEP_ERR_CONFIG = 2,     /* unsupported configuration (bs != 1, n < 2, ...) */
+  PSTEP_ERR_CAPACITY = 3,   /* more particles than the handle was created for */
+  PSTEP_ERR_STATE = 4,      /* call out of order (e.g. stage before fields are bound) */
+  PSTEP_ERR_CUDA = 5,       /* a CUDA runtime call failed; see pstep_last_error */
+  PSTEP_ERR_NONFINITE = 6,  /* NaN/Inf found in particle state or fields */
+  PSTEP_ERR_RANGE = 7,      /* a particle position outside [0, L] (or at L, where the
+                               reference indexes past its ghost layer) */
+  PSTEP_ERR_MOVE = 8,       /* a particle moved more than one cell in one stage */
+  PSTEP_ERR_NOMEM = 9,      /* device allocation failed */
+  PSTEP_ERR_TIMEOUT = 10    /* a bounded device-side wait gave up */
+} pstep_status;
+
+enum { PSTEP_FP64 = 0, PSTEP_FP32 = 1 };
+
+/* config.flags */
+enum {
+  PSTEP_TRACK_ORDER = 1,   /* keep the reference's particle order for downloads (FP64 only) */
+  PSTEP_CHECK_INPUTS = 2   /* validate uploads (finite, in range) before use */
+};
+
+/* Scalars of params.h that the particle step reads (params.cpp:22-56). The
+ * derived values Tp and mp are passed as the reference computes them. */
+typedef struct pstep_config {
+  int32_t nx, ny, nz;        /* global cells per side: Nx_tot, Ny_tot, Nz_tot */
+  int32_t bs;                /* ghost width; the reference's periodic box uses 1 */
+  int32_t twc;               /* TWC: deposit momentum (particle.cpp:498, grid.cpp:671) */
+  int32_t particle_gravity;  /* ParticleGravity (particle.cpp:376-378) */
+  int32_t precision;         /* PSTEP_FP64 or PSTEP_FP32 */
+  int32_t flags;             /* PSTEP_TRACK_ORDER | PSTEP_CHECK_INPUTS */
+  int64_t capacity;          /* maximum number of particles */
+  double lx, ly, lz;         /* box size */
+  double dt;                 /* time step */
+  double tp;                 /* momentum relaxation time Tp = Rhop*Dp^2/(18*Mu0) */
+  double mp;                 /* particle mass mp = Rhop*PI*Dp^3/6 */
+  double dp, nu, k, epsilonp, i0, cvp;  /* Dp, Nu, k, epsilon_p, I0, Cvp */
+  double gx, gy, gz;         /* gravity (used when particle_gravity != 0) */
+} pstep_config;
+
+/* particle array ids for pstep_get_particle_array / pstep_set_particle_array */
+enum {
+  PSTEP_X = 0, PSTEP_Y, PSTEP_Z, PSTEP_U, PSTEP_V, PSTEP_W, PSTEP_T,                 /* base state */
+  PSTEP_X_INT, PSTEP_Y_INT, PSTEP_Z_INT, PSTEP_U_INT, PSTEP_V_INT, PSTEP_W_INT, PSTEP_T_INT,
+  PSTEP_X_NEW, PSTEP_Y_NEW, PSTEP_Z_NEW, PSTEP_U_NEW, PSTEP_V_NEW, PSTEP_W_NEW, PSTEP_T_NEW,
+  PSTEP_X_NP1, PSTEP_Y_NP1, PSTEP_Z_NP1, PSTEP_U_NP1, PSTEP_V_NP1, PSTEP_W_NP1, PSTEP_T_NP1,
+  PSTEP_RHS_T,               /* particle.h:116 */
+  PSTEP_FLAG,                /* int32 particle id (particle.h:119) */
+  PSTEP_NUM_ARRAYS
+};
+
+/* deposited field ids for pstep_get_field (ghosted (nx+2)(ny+2)(nz+2) doubles) */
+enum {
+  PSTEP_FIELD_C = 0,         /* concentration, part2gas_concentration (particle.cpp:526-559) */
+  PSTEP_FIELD_RU_X,          /* RHS_RU.x, part2gas_velocity (particle.cpp:498-524) */
+  PSTEP_FIELD_RU_Y,
+  PSTEP_FIELD_RU_Z,
+  PSTEP_FIELD_PART_TEMP,     /* RHS_Part_Temp, part2gas_Temp_int/new (particle.cpp:586-658) */
+  PSTEP_NUM_FIELDS
+};
+
+/* Create a handle on the current CUDA device (replaces particle::particle,
+ * particle.cpp:14-40; allocates all device storage up front). */
+int pstep_create(const pstep_config *cfg, pstep_handle *out);
+/* Release everything (particle::~particle, particle.cpp:42-56). */
+int pstep_destroy(pstep_handle h);
+/* Stream for all work of this handle (cudaStream_t; 0 = legacy default). */
+int pstep_set_stream(pstep_handle h, void *cuda_stream);
+
+/* Set the base particle state x,u,T and flag for n particles (the reference's
+ * load_random / Load_All leave these in the public vectors, particle.cpp:919-999).
+ * Also does the particle part of grid::Initialize (grid.cpp:207-221):
+ * *_int = *_np1 = base. */
+int pstep_upload_particles(pstep_handle h, int64_t n, const double *x, const double *y, const double *z,
+                           const double *u, const double *v, const double *w, const double *t,
+                           const int32_t *flag, int on_device);
+/* Optional per-particle momentum relaxation time (same order as the upload);
+ * replaces the scalar Tp for every particle. NULL restores the scalar. */
+int pstep_set_tau_p(pstep_handle h, const double *tau_p, int on_device);
+int64_t pstep_num_particles(pstep_handle h);
+
+/* Gas fields, ghosted layout. The velocity is U = RU_int/Rho_face (grid.cpp:662),
+ * the temperature T = (P0_new/R)/Rho_new (grid.cpp:676); both are formed by the
+ * caller as in the reference. Host pointers are copied; device pointers are
+ * read in place and must stay valid until the next bind. */
+int pstep_bind_velocity(pstep_handle h, const double *ux, const double *uy, const double *uz, int on_device);
+int pstep_bind_temperature(pstep_handle h, const double *t, int on_device);
+
+/* grid.cpp:223-226: gas2part_Temp_int + Compute_RHS_Temp_int + part2gas_Temp_int
+ * (RHS_Part_Temp is then available through pstep_get_field). Needs the bound
+ * temperature. */
+int pstep_prime(pstep_handle h);
+
+/* One RK4 stage (k = 0..3) of grid::Update_Particle (grid.cpp:659-680), split as
+ * the reference's particle.h calls group:
+ *   interp_advance_deposit  gas2part_velocity, update_position, update_velocity,
+ *                           update_Temp, part2gas_concentration, part2gas_velocity
+ *   wrap                    Send_Recv (periodic wrap + the reference's reordering)
+ *   stage_temp              gas2part_Temp_new, Compute_RHS_Temp_new,
+ *                           part2gas_Temp_new, and the interior mean of
+ *                           RHS_Part_Temp (grid.cpp:541)
+ * pre/post are the RK4 coefficients of grid.cpp:16-23 for stage k. */
+int pstep_stage_interp_advance_deposit(pstep_handle h, int k, double pre, double post);
+int pstep_wrap(pstep_handle h);
+int pstep_stage_temp(pstep_handle h);
+/* the three above in order */
+int pstep_stage(pstep_handle h, int k, double pre, double post);
+/* grid::TimeAdvance_RK4, particle part (grid.cpp:705-712): *_int = *_new */
+int pstep_end_stage(pstep_handle h);
+/* grid::TimeAdvance, particle part (grid.cpp:315-325): base = *_np1; the
+ * particles are then reordered in device memory by cell (downloads keep the
+ * reference order when PSTEP_TRACK_ORDER is set). */
+int pstep_end_step(pstep_handle h);
+/* nsteps full steps with the bound fields held fixed (4 x stage + end_stage,
+ * then end_step), standard RK4 coefficients. */
+int pstep_run(pstep_handle h, int nsteps);
+
+/* Copy a deposited field (ghosted layout) to dst. */
+int pstep_get_field(pstep_handle h, int field_id, double *dst, int on_device);
+/* RHS_Part_Temp.mean() of the last stage_temp/prime (tensor0.cpp:418-435, grid.cpp:541). */
+int pstep_energy_mean(pstep_handle h, double *out);
+/* Copy one particle array (PSTEP_X ... PSTEP_FLAG) to dst (int32 for PSTEP_FLAG),
+ * in the reference's order when PSTEP_TRACK_ORDER is set. */
+int pstep_get_particle_array(pstep_handle h, int array_id, void *dst, int on_device);
+
+/* Error reporting */
+const char *pstep_last_error(pstep_handle h);
+const char *pstep_status_string(int status);
+/* Device-side check word: the OR of PSTEP_ERR_* conditions seen by the kernels
+ * since the last call (non-finite values, out-of-range positions, moves of more
+ * than one cell). Synchronises the stream and clears the word. */
+int pstep_check(pstep_handle h, int32_t *flags_out);
+
+/* Per-phase kernel timing with CUDA events on the handle's stream (no host
+ * synchronisation while enabled). Phases: PSTEP_PHASE_*. pstep_profile_read
+ * synchronises, returns total ms and event-pair counts per phase, and resets. */
+enum {
+  PSTEP_PHASE_ADVANCE = 0,     /* interpolation + RK4 advance + wrap + T interpolation */
+  PSTEP_PHASE_DEPOSIT_INT,     /* concentration + momentum deposits, fold, refresh */
+  PSTEP_PHASE_ORDER,           /* reference-order bookkeeping of Send_Recv */
+  PSTEP_PHASE_SORT,            /* counting sort by node (CSR) */
+  PSTEP_PHASE_DEPOSIT_TEMP,    /* energy deposit, fold, refresh, interior mean */
+  PSTEP_PHASE_REORDER,         /* per-step reorder of particle storage */
+  PSTEP_NUM_PHASES
+};
+int pstep_profile(pstep_handle h, int enable);
+int pstep_profile_read(pstep_handle h, double *ms, int64_t *counts, int nphases);
+
+/* Timing of the last pstep_run on the handle's stream (CUDA events): total ms. */
+int pstep_last_run_ms(pstep_handle h, double *ms);
+/* Number of kernel launches enqueued by this handle since creation. */
+int64_t pstep_launch_count(pstep_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

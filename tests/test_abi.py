@@ -1,0 +1,62 @@
+"""The drop-in boundary: libpstep.so builds, loads without a GPU, and exports
+every entry point include/pstep.h declares (no compute calls here)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+import helpers  # noqa: F401  (sets sys.path)
+from first_repo_gb300 import _lib, pstep
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pstep_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_binding_surface():
+    names = declared("pstep.h")
+    assert set(pstep.EXPORTS) <= set(names)
+
+
+def test_library_exports_every_declared_symbol(built_cuda):
+    lib = ctypes.CDLL(_lib.path("libpstep.so"))
+    for name in declared("pstep.h"):
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.path("libpstep.so")], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\b(pstep_[a-z0-9_]+)\b", out))
+    for name in declared("pstep.h"):
+        assert name in exported, name
+
+
+def test_status_strings_without_device(built_cuda):
+    L = pstep.lib()
+    assert L.pstep_status_string(0) == b"ok"
+    assert L.pstep_status_string(3) == b"capacity exceeded"
+
+
+def test_create_rejects_bad_config_without_touching_device(built_cuda):
+    L = pstep.lib()
+    c = pstep.Config()
+    c.nx = c.ny = c.nz = 8
+    c.bs = 2  # the reference's box uses bs = 1
+    c.lx = c.ly = c.lz = 1.0
+    c.dt = 1e-3
+    h = ctypes.c_void_p()
+    assert L.pstep_create(ctypes.byref(c), ctypes.byref(h)) == 2
+    c.bs = 1
+    c.nx = 1
+    assert L.pstep_create(ctypes.byref(c), ctypes.byref(h)) == 2
+    assert L.pstep_create(None, ctypes.byref(h)) == 1
+
+
+def test_null_handle_is_an_error(built_cuda):
+    L = pstep.lib()
+    assert L.pstep_prime(None) == 1
+    assert L.pstep_end_step(None) == 1
+    assert L.pstep_num_particles(None) == -1
