@@ -45,6 +45,11 @@ from first_repo_gb300 import config, gen  # noqa: E402
 #            k=1..3 also read *_int(7) and *_np1(7) = +112 B;  fields U(3) and T read once per launch.
 FP64_ADVANCE_BYTES = {0: 92 + 173, 1: 92 + 173 + 112, 2: 92 + 173 + 112, 3: 92 + 173 + 112}
 FP64_ADVANCE_CELL_BYTES = 4 * 8
+# FP32 form: a particle set is 32 B (cell + 3 offsets + u,v,w,T).
+#   k=0 reads base + RHS_T = 36 B; writes *_new + *_np1 + RHS_u(3) + RHS_T = 80 B
+#   k=1..3 read base, *_int, *_np1 + RHS_T = 100 B; write 80 B.  fp32 fields U(3), T once per launch.
+FP32_ADVANCE_BYTES = {0: 36 + 80, 1: 100 + 80, 2: 100 + 80, 3: 100 + 80}
+FP32_ADVANCE_CELL_BYTES = 4 * 4
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
@@ -124,12 +129,15 @@ def make_inputs(wl, dp_over_dx=0.1, mass_loading=0.2):
     return case, bp, fields, time.time() - t0
 
 
+_PINNED = []  # keeps the pinned host allocations alive
+
+
 def pinned_like(a: np.ndarray) -> np.ndarray:
     import torch
     t = torch.empty(a.shape, dtype=torch.float64 if a.dtype == np.float64 else torch.int32, pin_memory=True)
+    _PINNED.append(t)
     out = t.numpy()
     out[...] = a
-    out._torch_ref = t  # noqa: keep the pinned allocation alive
     return out
 
 
@@ -264,7 +272,9 @@ def main():
     dom_ms, dom_cnt = prof[dom]
     roof = None
     if dom == "advance" and dom_cnt:
-        per_launch = n * sum(FP64_ADVANCE_BYTES.values()) / 4.0 + FP64_ADVANCE_CELL_BYTES * (wl.n + 2) ** 3
+        pb, cb = (FP32_ADVANCE_BYTES, FP32_ADVANCE_CELL_BYTES) if form == pstep.FP32 else \
+            (FP64_ADVANCE_BYTES, FP64_ADVANCE_CELL_BYTES)
+        per_launch = n * sum(pb.values()) / 4.0 + cb * (wl.n + 2) ** 3
         achieved = per_launch / (dom_ms / dom_cnt / 1e3) / 1e9
         traffic = None
         tf_path = os.path.join(ROOT, "profiles", "ncu_traffic.json")

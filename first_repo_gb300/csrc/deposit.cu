@@ -1,13 +1,21 @@
-// Two-way-coupling deposition, FP64 drop-in form, as target-cell gathers.
+// Two-way-coupling deposition, FP64 drop-in form. No atomics anywhere: every
+// target value is a sum in a fixed order, so results are identical run to run.
 //
-// Each thread owns one target cell of the ghosted grid and walks the sorted
-// particles (CSR by node key) of the few nodes whose stencils reach it, merging
-// the node lists by the CSR's secondary key. With PSTEP_TRACK_ORDER that key is
-// the particle's position in the reference's vectors, so every cell receives
-// its contributions in exactly the order the reference's scatter loop adds them
-// (particle.cpp:498-658), from 0, with the reference's weight expressions; the
-// cumulative ghost fold and the ghost refresh then replay communicator.cpp's
-// single-rank sequence. No atomics: the result is the same on every run.
+// Fast path (k_dep_brick): one CTA per brick of B^3 target cells of the ghosted
+// grid. Its threads walk the CSR segments (particles sorted by node, then h,
+// then storage index) of the brick's nodes plus a one-node halo, form per-node
+// partial sums in shared memory -- the 8 trilinear offsets of a node, and the
+// face-normal partials of each trunc cell, added in 8 conflict-free phases (one
+// per h class) -- then every target cell sums its partials in a fixed order.
+// Halo nodes are walked by both neighbouring bricks; no cross-brick reduction.
+//
+// Reference-order path (PSTEP_REFERENCE_SUMS, k_dep_trilinear / k_dep_face):
+// each thread owns one target cell and merges the node lists by the particles'
+// positions in the reference's vectors, so every cell receives its
+// contributions in exactly the order the reference's scatter loop adds them
+// (particle.cpp:498-658), from 0, with the reference's weight expressions.
+// Either way the cumulative ghost fold and the ghost refresh then replay
+// communicator.cpp's single-rank sequence.
 //
 // Compiled with -fmad=false (see stage_f64.cu).
 #include "pstep_internal.cuh"
@@ -137,6 +145,132 @@ __global__ void k_dep_face(Geom G, DepIn d, double *__restrict__ out) {
   out[t] = acc;
 }
 
+// ---- fast path ----------------------------------------------------------------
+constexpr int kB = 8;                 // brick edge (target cells)
+constexpr int kB1 = kB + 1;           // trilinear node region edge [b, b+B]
+constexpr int kB2 = kB + 2;           // face node region edge [b-1, b+B]
+constexpr int kBrickThreads = 256;
+constexpr size_t kBrickSmem = (size_t)kB1 * kB1 * kB1 * (8 + 6) * sizeof(double);
+
+__device__ inline int32_t seg_lower_h(const DepIn &d, int32_t a, int32_t b, uint32_t hcls) {
+  // first position in [a, b) whose particle has h class >= hcls (segments are sorted by h)
+  while (a < b) {
+    int32_t m = (a + b) >> 1;
+    if ((d.key[pidx(d, m)] & 7u) < hcls) a = m + 1; else b = m;
+  }
+  return a;
+}
+
+// mode 0: concentration (weights) + face momentum partials at x_int; mode 1: weights * RHS_T
+__global__ void __launch_bounds__(kBrickThreads) k_dep_brick(Geom G, DepIn d, int mode, int twc,
+                                                             double *__restrict__ out_tri,
+                                                             double *__restrict__ out_x,
+                                                             double *__restrict__ out_y,
+                                                             double *__restrict__ out_z) {
+  extern __shared__ double sm[];
+  double *P = sm;                              // [kB1^3][8] trilinear partials of node b + l
+  double *F = sm + kB1 * kB1 * kB1 * 8;        // [kB1^3][6] face partials of trunc cell b - 1 + l
+  const int nbx = (G.g[0] + kB - 1) / kB, nby = (G.g[1] + kB - 1) / kB;
+  const int bx = (int)(blockIdx.x % nbx) * kB;
+  const int by = (int)((blockIdx.x / nbx) % nby) * kB;
+  const int bz = (int)(blockIdx.x / ((long long)nbx * nby)) * kB;
+
+  // trilinear: per-node partials for nodes [b, b+B]
+  for (int s = threadIdx.x; s < kB1 * kB1 * kB1; s += blockDim.x) {
+    const int lx = s % kB1, ly = (s / kB1) % kB1, lz = s / (kB1 * kB1);
+    const int ni = bx + lx, nj = by + ly, nk = bz + lz;
+    double acc[8];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) acc[o] = 0.0;
+    if (node_ok(G, ni, nj, nk)) {
+      const long long n = glin(G, ni, nj, nk);
+      const int32_t a = d.cell_start[n], e = d.cell_start[n + 1];
+      for (int32_t q = a; q < e; ++q) {
+        const int32_t p = pidx(d, q);
+        const uint32_t key = d.key[p];
+        const double xl = xl_round(d.frac[0][p], (key >> 2) & 1);
+        const double yl = xl_round(d.frac[1][p], (key >> 1) & 1);
+        const double zl = xl_round(d.frac[2][p], key & 1);
+        const double v = mode ? d.val[0][p] : 1.0;
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+          const double fx = (o & 4) ? (1 - xl) : xl;
+          const double fy = (o & 2) ? (1 - yl) : yl;
+          const double fz = (o & 1) ? (1 - zl) : zl;
+          double w = fx * fy * fz;
+          if (mode) w = w * v;
+          acc[o] += w;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < 8; ++o) P[s * 8 + o] = acc[o];
+  }
+  const bool faces = (mode == 0) && twc;
+  if (faces) {
+    for (int s = threadIdx.x; s < kB1 * kB1 * kB1 * 6; s += blockDim.x) F[s] = 0.0;
+  }
+  __syncthreads();
+  // face partials: trunc cell c = node - h, one h class per phase (distinct nodes -> distinct cells)
+  if (faces) {
+    for (uint32_t hc = 0; hc < 8; ++hc) {
+      const int hx = (hc >> 2) & 1, hy = (hc >> 1) & 1, hz = hc & 1;
+      for (int s = threadIdx.x; s < kB2 * kB2 * kB2; s += blockDim.x) {
+        const int lx = s % kB2, ly = (s / kB2) % kB2, lz = s / (kB2 * kB2);
+        const int cx = lx - hx, cy = ly - hy, cz = lz - hz;  // cell slot: cell = b - 1 + c
+        if (cx < 0 || cy < 0 || cz < 0 || cx >= kB1 || cy >= kB1 || cz >= kB1) continue;
+        const int ni = bx - 1 + lx, nj = by - 1 + ly, nk = bz - 1 + lz;
+        if (!node_ok(G, ni, nj, nk)) continue;
+        const long long n = glin(G, ni, nj, nk);
+        const int32_t a0 = d.cell_start[n], e0 = d.cell_start[n + 1];
+        if (a0 == e0) continue;
+        const int32_t a = seg_lower_h(d, a0, e0, hc);
+        const int32_t e = seg_lower_h(d, a, e0, hc + 1);
+        if (a == e) continue;
+        double s0x = 0, s1x = 0, s0y = 0, s1y = 0, s0z = 0, s1z = 0;
+        for (int32_t q = a; q < e; ++q) {
+          const int32_t p = pidx(d, q);
+          const double xl = d.frac[0][p], yl = d.frac[1][p], zl = d.frac[2][p];
+          const double ru = d.val[0][p], rv = d.val[1][p], rw = d.val[2][p];
+          s1x += xl * ru;
+          s0x += (1 - xl) * ru;
+          s1y += yl * rv;
+          s0y += (1 - yl) * rv;
+          s1z += zl * rw;
+          s0z += (1 - zl) * rw;
+        }
+        double *f = F + ((cz * kB1 + cy) * kB1 + cx) * 6;
+        f[0] += s0x; f[1] += s1x; f[2] += s0y; f[3] += s1y; f[4] += s0z; f[5] += s1z;
+      }
+      __syncthreads();
+    }
+  }
+  // targets of the brick
+  for (int s = threadIdx.x; s < kB * kB * kB; s += blockDim.x) {
+    const int lx = s % kB, ly = (s / kB) % kB, lz = s / (kB * kB);
+    const int ti = bx + lx, tj = by + ly, tk = bz + lz;
+    if (ti >= G.g[0] || tj >= G.g[1] || tk >= G.g[2]) continue;
+    double acc = 0.0;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int ox = (o >> 2) & 1, oy = (o >> 1) & 1, oz = o & 1;
+      acc += P[(((lz + oz) * kB1 + (ly + oy)) * kB1 + (lx + ox)) * 8 + o];
+    }
+    const long long t = glin(G, ti, tj, tk);
+    out_tri[t] = acc;
+    if (faces) {
+      // cell slot of target cell t is l + 1; its lower neighbour in dimension D is l
+      const double *ft = F + (((lz + 1) * kB1 + (ly + 1)) * kB1 + (lx + 1)) * 6;
+      const double *fxm = F + (((lz + 1) * kB1 + (ly + 1)) * kB1 + lx) * 6;
+      const double *fym = F + (((lz + 1) * kB1 + ly) * kB1 + (lx + 1)) * 6;
+      const double *fzm = F + ((lz * kB1 + (ly + 1)) * kB1 + (lx + 1)) * 6;
+      out_x[t] = fxm[1] + ft[0];
+      out_y[t] = fym[3] + ft[2];
+      out_z[t] = fzm[5] + ft[4];
+    }
+  }
+}
+
 // communicator.cpp:422-511 on one rank, one phase per launch; nf fields at once
 struct FieldSet {
   double *f[5];
@@ -262,7 +396,7 @@ DepIn make_in(pstep_ctx *h, const Csr &csr, double *const frac[3], const uint32_
   DepIn d;
   d.cell_start = csr.cell_start;
   d.sidx = csr.identity ? nullptr : csr.sidx;
-  d.order = (h->cfg.flags & PSTEP_TRACK_ORDER) ? h->ref_of_phys : nullptr;
+  d.order = ((h->cfg.flags & PSTEP_TRACK_ORDER) && (h->cfg.flags & PSTEP_REFERENCE_SUMS)) ? h->ref_of_phys : nullptr;
   for (int q = 0; q < 3; ++q) d.frac[q] = frac[q];
   d.key = key;
   d.val[0] = v0;
@@ -273,12 +407,22 @@ DepIn make_in(pstep_ctx *h, const Csr &csr, double *const frac[3], const uint32_
 
 }  // namespace
 
+// refresh: 0 fold only, 1 fold then refresh, 2 refresh only (interior already periodic)
 int fold_fields(pstep_ctx *h, double *const *f, int nf, int refresh) {
   const Geom &G = h->geom;
   FieldSet fs;
   fs.nf = nf;
   for (int q = 0; q < nf; ++q) fs.f[q] = f[q];
   long long plane = (long long)G.g[0] * G.g[1];
+  if (refresh == 2) {
+    k_refresh_x<<<blocks_for((long long)G.n[1] * G.n[2] * nf), kThreads, 0, h->stream>>>(G, fs);
+    PSTEP_LAUNCHED(h);
+    k_refresh_y<<<blocks_for((long long)G.g[0] * G.n[2] * nf), kThreads, 0, h->stream>>>(G, fs);
+    PSTEP_LAUNCHED(h);
+    k_refresh_z<<<blocks_for(plane * nf), kThreads, 0, h->stream>>>(G, fs);
+    PSTEP_LAUNCHED(h);
+    return PSTEP_OK;
+  }
   k_fold_z<<<blocks_for(plane * nf), kThreads, 0, h->stream>>>(G, fs);
   PSTEP_LAUNCHED(h);
   k_fold_y<<<blocks_for((long long)G.g[0] * G.n[2] * nf), kThreads, 0, h->stream>>>(G, fs);
@@ -307,12 +451,34 @@ int interior_mean(pstep_ctx *h, const double *f, double *out_dev) {
 }
 
 // part2gas_Temp_int/new: deposit RHS_T with the records of csr/frac/key, fold, refresh, mean.
+bool reference_sums(const pstep_ctx *h) {
+  return (h->cfg.flags & PSTEP_TRACK_ORDER) && (h->cfg.flags & PSTEP_REFERENCE_SUMS);
+}
+
+int brick_launch(pstep_ctx *h, const DepIn &d, int mode, double *tri, double *ox, double *oy, double *oz) {
+  const Geom &G = h->geom;
+  static bool attr = false;
+  if (!attr) {
+    PSTEP_CUDA(cudaFuncSetAttribute(k_dep_brick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBrickSmem));
+    attr = true;
+  }
+  const long long nb = (long long)((G.g[0] + kB - 1) / kB) * ((G.g[1] + kB - 1) / kB) * ((G.g[2] + kB - 1) / kB);
+  k_dep_brick<<<(unsigned)nb, kBrickThreads, kBrickSmem, h->stream>>>(G, d, mode, h->cfg.twc, tri, ox, oy, oz);
+  PSTEP_LAUNCHED(h);
+  return PSTEP_OK;
+}
+
 int deposit_temperature(pstep_ctx *h, const Csr &csr, double *const frac[3], const uint32_t *key) {
   const Geom &G = h->geom;
   DepIn d = make_in(h, csr, frac, key, h->s.rhs_t, nullptr, nullptr);
   double *out = h->dep[PSTEP_FIELD_PART_TEMP];
-  k_dep_trilinear<<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, 1, out);
-  PSTEP_LAUNCHED(h);
+  if (reference_sums(h)) {
+    k_dep_trilinear<<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, 1, out);
+    PSTEP_LAUNCHED(h);
+  } else {
+    int rc = brick_launch(h, d, 1, out, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+  }
   double *fl[1] = {out};
   int rc = fold_fields(h, fl, 1, 1);
   if (rc) return rc;
@@ -323,6 +489,21 @@ int deposit_temperature(pstep_ctx *h, const Csr &csr, double *const frac[3], con
 int f64_deposit_int(pstep_ctx *h) {
   const Geom &G = h->geom;
   DepIn d = make_in(h, h->csr_prev, h->s.frac_prev, h->s.key_prev, h->s.rhs_u[0], h->s.rhs_u[1], h->s.rhs_u[2]);
+  if (!reference_sums(h)) {
+    int rc = brick_launch(h, d, 0, h->dep[PSTEP_FIELD_C], h->dep[PSTEP_FIELD_RU_X], h->dep[PSTEP_FIELD_RU_Y],
+                          h->dep[PSTEP_FIELD_RU_Z]);
+    if (rc) return rc;
+    double *c1[1] = {h->dep[PSTEP_FIELD_C]};
+    rc = fold_fields(h, c1, 1, 0);  // the reference does not refresh C's ghosts
+    if (rc) return rc;
+    if (h->cfg.twc) {
+      double *ru[3] = {h->dep[PSTEP_FIELD_RU_X], h->dep[PSTEP_FIELD_RU_Y], h->dep[PSTEP_FIELD_RU_Z]};
+      return fold_fields(h, ru, 3, 1);
+    }
+    for (int q = PSTEP_FIELD_RU_X; q <= PSTEP_FIELD_RU_Z; ++q)
+      PSTEP_CUDA(cudaMemsetAsync(h->dep[q], 0, sizeof(double) * G.gsize, h->stream));
+    return PSTEP_OK;
+  }
   k_dep_trilinear<<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, 0, h->dep[PSTEP_FIELD_C]);
   PSTEP_LAUNCHED(h);
   double *c1[1] = {h->dep[PSTEP_FIELD_C]};

@@ -131,7 +131,7 @@ void release(pstep_ctx *h) {
   for (int d = 0; d < 3; ++d) { dfree(h->s.frac_prev[d]); dfree(h->s.frac_new[d]); dfree(h->s.rhs_u[d]); }
   dfree(h->s.key_prev); dfree(h->s.key_new);
   dfree(h->csr_prev.cell_start); dfree(h->csr_prev.sidx); dfree(h->csr_new.cell_start); dfree(h->csr_new.sidx);
-  dfree(h->counts); dfree(h->cursor); dfree(h->scan_blocks);
+  dfree(h->counts); dfree(h->cursor); dfree(h->scan_blocks); dfree(h->big_list); dfree(h->big_count);
   void *pt = h->perm_tmp; if (pt) cudaFree(pt); h->perm_tmp = nullptr;
   for (int d = 0; d < 3; ++d) dfree(h->own_u[d]);
   dfree(h->own_t);
@@ -164,9 +164,6 @@ int alloc_all(pstep_ctx *h) {
     }
     TRY(dalloc(h, h->s.key_prev, cap)); TRY(dalloc(h, h->s.key_new, cap));
     TRY(dalloc(h, h->csr_prev.sidx, cap)); TRY(dalloc(h, h->csr_new.sidx, cap));
-    double *pt = nullptr;
-    TRY(dalloc(h, pt, cap));
-    h->perm_tmp = pt;
     if (h->cfg.flags & PSTEP_TRACK_ORDER) {
       TRY(dalloc(h, h->ref_of_phys, cap)); TRY(dalloc(h, h->phys_of_ref, cap));
       TRY(dalloc(h, h->leave_code, cap));
@@ -179,8 +176,14 @@ int alloc_all(pstep_ctx *h) {
       PSTEP_LAUNCHED(h);
     }
   }
+  {  // permutation / download scratch, both forms
+    double *pt = nullptr;
+    TRY(dalloc(h, pt, cap));
+    h->perm_tmp = pt;
+  }
   TRY(dalloc(h, h->csr_prev.cell_start, gs + 1)); TRY(dalloc(h, h->csr_new.cell_start, gs + 1));
   TRY(dalloc(h, h->counts, gs)); TRY(dalloc(h, h->cursor, gs));
+  TRY(dalloc(h, h->big_list, gs)); TRY(dalloc(h, h->big_count, 1));
   int64_t scan_n = (int64_t)gs + 1;
   if ((int64_t)cap > scan_n) scan_n = (int64_t)cap;
   h->scan_nblocks = scan_blocks_needed(scan_n) + 1;
@@ -328,6 +331,7 @@ int pstep_upload_particles(pstep_handle h, int64_t n, const double *x, const dou
   if (h->s.itp) dfree(h->s.itp);  // a new population drops any per-particle tau_p
   h->int_is_base = 1;
   h->np1_is_base = 1;
+  h->new_is_zero = 1;  // the reference's *_new vectors are zero-filled until the first stage writes them
   h->csr_prev.identity = 0;
   if (h->cfg.flags & PSTEP_TRACK_ORDER) TRY(order_init(h));
   if (h->cfg.flags & PSTEP_CHECK_INPUTS && !on_device) {
@@ -422,6 +426,8 @@ int pstep_stage_interp_advance_deposit(pstep_handle h, int k, double pre, double
   if (h->phase != 0) return fail(h, PSTEP_ERR_STATE, "previous stage not finished (pstep_end_stage)");
   if ((k == 0) != (h->int_is_base != 0)) return fail(h, PSTEP_ERR_STATE, "stage index out of sequence");
   h->cur_k = k;
+  h->new_is_zero = 0;
+  h->np1_is_base = 0;  // the stage writes *_np1
   if (is_f32(h)) {
     TRY(f32_stage(h, k, pre, post));
     h->phase = 1;
@@ -601,12 +607,20 @@ int pstep_get_particle_array(pstep_handle h, int id, void *dst, int on_device) {
       src = h->s.base[id - PSTEP_X];
     } else if (id <= PSTEP_T_INT) {
       int q = id - PSTEP_X_INT;
-      src = h->int_is_base ? h->s.base[q] : h->s.sint[q];
+      // during stage 0 the unshifted *_int positions are in sint (the base may be wrapped)
+      src = (h->int_is_base && !(q < 3 && h->phase != 0)) ? h->s.base[q] : h->s.sint[q];
     } else if (id <= PSTEP_T_NEW) {
       int q = id - PSTEP_X_NEW;
-      // after end_stage the reference's *_new equal *_int; at the start of a step, the base
-      if (h->int_is_base) src = h->s.base[q];
-      else src = (h->phase == 0) ? h->s.sint[q] : h->s.snew[q];
+      if (h->new_is_zero) {
+        PSTEP_CUDA(cudaMemsetAsync(h->perm_tmp, 0, sizeof(double) * n, h->stream));
+        PSTEP_CUDA(cudaMemcpyAsync(dst, h->perm_tmp, sizeof(double) * n, kind_out(on_device), h->stream));
+        if (!on_device) PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+        return PSTEP_OK;
+      }
+      // within a stage: the new values; after end_stage the reference's *_new equal *_int;
+      // at the start of a step, the base
+      if (h->phase != 0) src = h->s.snew[q];
+      else src = h->int_is_base ? h->s.base[q] : h->s.sint[q];
     } else if (id <= PSTEP_T_NP1) {
       int q = id - PSTEP_X_NP1;
       src = h->np1_is_base ? h->s.base[q] : h->s.np1[q];

@@ -59,6 +59,8 @@ struct F64State {
   double *rhs_u[3];              // RHS_u at x_int of the current stage
 };
 
+struct F32Form;
+
 // Counting-sort CSR by node key.
 struct Csr {
   int32_t *cell_start;  // gsize + 1
@@ -80,6 +82,7 @@ struct pstep_ctx {
   // FP64 state
   pstep::F64State s;
   pstep::Csr csr_prev, csr_new;
+  int new_is_zero;  // no stage has run since the upload: *_new read as zeros
   int int_is_base;  // *_int equal base (start of step): read base
   int np1_is_base;  // *_np1 equal base
 
@@ -87,6 +90,8 @@ struct pstep_ctx {
   int32_t *counts;      // gsize
   int32_t *cursor;      // gsize
   int32_t *scan_blocks; // block sums
+  int32_t *big_list;    // nodes with long segments (gsize)
+  int32_t *big_count;   // device counter
   int64_t scan_nblocks;
   // permutation scratch (per-step reorder)
   void *perm_tmp;
@@ -120,7 +125,7 @@ struct pstep_ctx {
   int cur_k;
 
   // FP32 form (stage_f32.cu)
-  struct F32Form *f32;
+  pstep::F32Form *f32;
 
   struct Prof *prof;  // per-phase event pairs (pstep_profile)
 
@@ -161,6 +166,10 @@ int f64_deposit_int(pstep_ctx *h);
 int f64_stage_temp(pstep_ctx *h);
 int f64_reorder(pstep_ctx *h);
 int sort_by_node(pstep_ctx *h, const uint32_t *keys, Csr &out);
+int csr_sort(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, const int32_t *order, int32_t *cell_start,
+             int32_t *sidx);
+template <typename T>
+__global__ void k_gather(const T *__restrict__ src, const int32_t *__restrict__ idx, int64_t n, T *__restrict__ dst);
 int fold_cum(pstep_ctx *h, double *f);
 int refresh_ghosts(pstep_ctx *h, double *f);
 int interior_mean(pstep_ctx *h, const double *f, double *out_dev);

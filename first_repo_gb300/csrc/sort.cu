@@ -13,10 +13,10 @@ namespace {
 constexpr int kScanItems = 16;                       // per thread
 constexpr int kScanTile = kThreads * kScanItems;     // per block
 
-__global__ void k_count(const uint32_t *__restrict__ keys, int64_t n, int32_t *__restrict__ counts) {
+__global__ void k_count(const uint32_t *__restrict__ keys, int shift, int64_t n, int32_t *__restrict__ counts) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool valid = i < n;
-  uint32_t node = valid ? (keys[i] >> 3) : 0xffffffffu;
+  uint32_t node = valid ? (keys[i] >> shift) : 0xffffffffu;
   // warp-aggregated increments: lanes with the same node add once
   unsigned active = __ballot_sync(0xffffffffu, valid);
   if (!valid) return;
@@ -108,11 +108,11 @@ __global__ void k_scan_apply(const int32_t *__restrict__ in, int64_t n, const in
   }
 }
 
-__global__ void k_scatter(const uint32_t *__restrict__ keys, int64_t n, int32_t *__restrict__ cursor,
+__global__ void k_scatter(const uint32_t *__restrict__ keys, int shift, int64_t n, int32_t *__restrict__ cursor,
                           int32_t *__restrict__ sidx) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool valid = i < n;
-  uint32_t node = valid ? (keys[i] >> 3) : 0xffffffffu;
+  uint32_t node = valid ? (keys[i] >> shift) : 0xffffffffu;
   unsigned active = __ballot_sync(0xffffffffu, valid);
   if (!valid) return;
   unsigned peers = __match_any_sync(active, node);
@@ -125,33 +125,114 @@ __global__ void k_scatter(const uint32_t *__restrict__ keys, int64_t n, int32_t 
   sidx[basepos + rank] = (int32_t)i;
 }
 
-// Order every node's segment by the secondary key (insertion sort; segments are short).
-__global__ void k_segsort(const int32_t *__restrict__ cell_start, int64_t gsize, int32_t *__restrict__ sidx,
-                          const int32_t *__restrict__ sortkey) {
+// Order every node's segment by a 64-bit secondary key: short segments (<= kSmallSeg)
+// by one thread (insertion sort), longer ones are listed for k_segsort_big.
+constexpr int kSmallSeg = 16;
+constexpr int kBigSegMax = 16384;  // per-node particles sortable on chip (12 B each in shared memory)
+
+__device__ inline uint64_t seckey(const int32_t *__restrict__ order, const uint32_t *__restrict__ keys, int32_t v) {
+  // an explicit secondary key (reference position, or particle id), else (h bits, storage index)
+  if (order) return (uint64_t)(uint32_t)order[v];
+  return ((uint64_t)(keys[v] & 7u) << 32) | (uint32_t)v;
+}
+
+__global__ void k_segsort_small(const int32_t *__restrict__ cell_start, int64_t gsize, int32_t *__restrict__ sidx,
+                                const int32_t *__restrict__ order, const uint32_t *__restrict__ keys,
+                                int32_t *__restrict__ big_list, int32_t *__restrict__ big_count,
+                                int32_t *__restrict__ err) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= gsize) return;
   int32_t a = cell_start[c], b = cell_start[c + 1];
-  if (b - a < 2) return;
-  for (int32_t p = a + 1; p < b; ++p) {
-    int32_t v = sidx[p];
-    int32_t kv = sortkey ? sortkey[v] : v;
-    int32_t q = p - 1;
-    while (q >= a) {
-      int32_t u = sidx[q];
-      int32_t ku = sortkey ? sortkey[u] : u;
-      if (ku <= kv) break;
-      sidx[q + 1] = u;
+  int32_t len = b - a;
+  if (len < 2) return;
+  if (len > kSmallSeg) {
+    if (len > kBigSegMax) atomicOr(err, kErrCapacity);
+    int32_t slot = atomicAdd(big_count, 1);
+    big_list[slot] = (int32_t)c;
+    return;
+  }
+  int32_t v[kSmallSeg];
+  uint64_t k[kSmallSeg];
+  for (int q = 0; q < len; ++q) {
+    v[q] = sidx[a + q];
+    k[q] = seckey(order, keys, v[q]);
+  }
+  for (int p = 1; p < len; ++p) {
+    int32_t vv = v[p];
+    uint64_t kv = k[p];
+    int q = p - 1;
+    while (q >= 0 && k[q] > kv) {
+      k[q + 1] = k[q];
+      v[q + 1] = v[q];
       --q;
     }
-    sidx[q + 1] = v;
+    k[q + 1] = kv;
+    v[q + 1] = vv;
+  }
+  for (int q = 0; q < len; ++q) sidx[a + q] = v[q];
+}
+
+// one block per listed long segment: bitonic sort in shared memory
+__global__ void __launch_bounds__(512) k_segsort_big(const int32_t *__restrict__ cell_start, int32_t *__restrict__ sidx,
+                                                     const int32_t *__restrict__ order,
+                                                     const uint32_t *__restrict__ keys,
+                                                     const int32_t *__restrict__ big_list,
+                                                     const int32_t *__restrict__ big_count) {
+  extern __shared__ unsigned char smraw[];
+  uint64_t *sk = (uint64_t *)smraw;
+  int32_t *sv = (int32_t *)(sk + kBigSegMax);
+  const int32_t nbig = *big_count;
+  for (int32_t w = blockIdx.x; w < nbig; w += gridDim.x) {
+    const int32_t c = big_list[w];
+    const int32_t a = cell_start[c], b = cell_start[c + 1];
+    const int32_t len = b - a;
+    if (len > kBigSegMax) continue;  // reported by k_segsort_small
+    int32_t m = 1;
+    while (m < len) m <<= 1;
+    for (int32_t q = threadIdx.x; q < m; q += blockDim.x) {
+      if (q < len) {
+        int32_t v = sidx[a + q];
+        sv[q] = v;
+        sk[q] = seckey(order, keys, v);
+      } else {
+        sv[q] = -1;
+        sk[q] = ~0ull;
+      }
+    }
+    __syncthreads();
+    for (int32_t kk = 2; kk <= m; kk <<= 1) {
+      for (int32_t j = kk >> 1; j > 0; j >>= 1) {
+        for (int32_t q = threadIdx.x; q < m; q += blockDim.x) {
+          int32_t r = q ^ j;
+          if (r > q) {
+            bool up = (q & kk) == 0;
+            uint64_t x = sk[q], y = sk[r];
+            if ((x > y) == up) {
+              sk[q] = y; sk[r] = x;
+              int32_t t = sv[q]; sv[q] = sv[r]; sv[r] = t;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    for (int32_t q = threadIdx.x; q < len; q += blockDim.x) sidx[a + q] = sv[q];
+    __syncthreads();
   }
 }
+
+}  // namespace
 
 template <typename T>
 __global__ void k_gather(const T *__restrict__ src, const int32_t *__restrict__ idx, int64_t n, T *__restrict__ dst) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[idx[i]];
 }
+template __global__ void k_gather<float>(const float *, const int32_t *, int64_t, float *);
+template __global__ void k_gather<uint32_t>(const uint32_t *, const int32_t *, int64_t, uint32_t *);
+template __global__ void k_gather<int32_t>(const int32_t *, const int32_t *, int64_t, int32_t *);
+
+namespace {
 
 __global__ void k_invert(const int32_t *__restrict__ ref_of_phys, int64_t n, int32_t *__restrict__ phys_of_ref) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -179,24 +260,38 @@ int exclusive_scan(pstep_ctx *h, const int32_t *in, int64_t n, int32_t *out, int
 
 int64_t scan_blocks_needed(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 
-int sort_by_node(pstep_ctx *h, const uint32_t *keys, Csr &out) {
-  const int64_t gsize = h->geom.gsize;
-  PSTEP_CUDA(cudaMemsetAsync(h->counts, 0, sizeof(int32_t) * gsize, h->stream));
+// Counting sort of the h->np particles by (keys[i] >> shift) into nkeys buckets:
+// cell_start[0..nkeys] and sidx, every bucket ordered by the secondary key.
+int csr_sort(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, const int32_t *order, int32_t *cell_start,
+             int32_t *sidx) {
+  PSTEP_CUDA(cudaMemsetAsync(h->counts, 0, sizeof(int32_t) * nkeys, h->stream));
   if (h->np > 0) {
-    k_count<<<blocks_for(h->np), kThreads, 0, h->stream>>>(keys, h->np, h->counts);
+    k_count<<<blocks_for(h->np), kThreads, 0, h->stream>>>(keys, shift, h->np, h->counts);
     PSTEP_LAUNCHED(h);
   }
-  int rc = exclusive_scan(h, h->counts, gsize, out.cell_start, h->cursor);
+  int rc = exclusive_scan(h, h->counts, nkeys, cell_start, h->cursor);
   if (rc) return rc;
   if (h->np > 0) {
-    k_scatter<<<blocks_for(h->np), kThreads, 0, h->stream>>>(keys, h->np, h->cursor, out.sidx);
+    k_scatter<<<blocks_for(h->np), kThreads, 0, h->stream>>>(keys, shift, h->np, h->cursor, sidx);
     PSTEP_LAUNCHED(h);
-    const int32_t *sk = (h->cfg.flags & PSTEP_TRACK_ORDER) ? h->ref_of_phys : nullptr;
-    k_segsort<<<blocks_for(gsize), kThreads, 0, h->stream>>>(out.cell_start, gsize, out.sidx, sk);
+    PSTEP_CUDA(cudaMemsetAsync(h->big_count, 0, sizeof(int32_t), h->stream));
+    k_segsort_small<<<blocks_for(nkeys), kThreads, 0, h->stream>>>(cell_start, nkeys, sidx, order, keys, h->big_list,
+                                                                    h->big_count, h->err_word);
+    PSTEP_LAUNCHED(h);
+    const size_t smem = (size_t)kBigSegMax * (sizeof(uint64_t) + sizeof(int32_t));
+    PSTEP_CUDA(cudaFuncSetAttribute(k_segsort_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_segsort_big<<<2 * h->num_sms, 512, smem, h->stream>>>(cell_start, sidx, order, keys, h->big_list, h->big_count);
     PSTEP_LAUNCHED(h);
   }
-  out.identity = 0;
   return PSTEP_OK;
+}
+
+int sort_by_node(pstep_ctx *h, const uint32_t *keys, Csr &out) {
+  const int32_t *order =
+      ((h->cfg.flags & PSTEP_TRACK_ORDER) && (h->cfg.flags & PSTEP_REFERENCE_SUMS)) ? h->ref_of_phys : nullptr;
+  int rc = csr_sort(h, keys, 3, h->geom.gsize, order, out.cell_start, out.sidx);
+  out.identity = 0;
+  return rc;
 }
 
 // Reorder particle storage by csr_prev.sidx (the sort of the positions the next

@@ -131,6 +131,12 @@ __global__ void __launch_bounds__(kThreads) k_advance(Geom G, F64State s, StageC
   const double vg = y_l * Uy[glin(G, ii, jj + 1, kk)] + (1 - y_l) * Uy[glin(G, ii, jj, kk)];
   const double wg = z_l * Uz[glin(G, ii, jj, kk + 1)] + (1 - z_l) * Uz[glin(G, ii, jj, kk)];
 
+  // at k = 0, *_int aliases the base state, which the wrap below may shift: keep the
+  // unshifted positions as *_int (the reference's MODE_L* leaves x_int alone)
+  if (K == 0) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) s.sint[d][i] = b[d];
+  }
   double nw[7];
   // update_position (particle.cpp:314-338)
 #pragma unroll

@@ -16,7 +16,7 @@ from . import _lib
 from .config import RK4_POST, RK4_PRE
 
 FP64, FP32 = 0, 1
-TRACK_ORDER, CHECK_INPUTS = 1, 2
+TRACK_ORDER, CHECK_INPUTS, REFERENCE_SUMS = 1, 2, 4
 
 ARRAY_IDS = {n: i for i, n in enumerate(
     ["x", "y", "z", "u", "v", "w", "T",

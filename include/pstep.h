@@ -24,7 +24,8 @@
  *  - PSTEP_FP64: the plain drop-in. Particle states, cell indices, the wrap and
  *    the particle order (the permutation that Send_Recv, particle.cpp:745-858,
  *    leaves behind) are bit-identical to the reference; deposited fields match
- *    it to round-off of a different (fixed, deterministic) summation order.
+ *    it to round-off of a different (fixed, deterministic) summation order, or
+ *    bit for bit with PSTEP_REFERENCE_SUMS.
  *  - PSTEP_FP32: mixed form. Positions as int32 cell + fp32 offset, fields and
  *    ODE arithmetic in fp32; deposits accumulated in fp64-class precision and
  *    written as fp64; balance reductions in fp64.
@@ -59,8 +60,11 @@ enum { PSTEP_FP64 = 0, PSTEP_FP32 = 1 };
 
 /* config.flags */
 enum {
-  PSTEP_TRACK_ORDER = 1,   /* keep the reference's particle order for downloads (FP64 only) */
-  PSTEP_CHECK_INPUTS = 2   /* validate uploads (finite, in range) before use */
+  PSTEP_TRACK_ORDER = 1,     /* keep the reference's particle order for downloads (FP64 only) */
+  PSTEP_CHECK_INPUTS = 2,    /* validate uploads (finite, in range) before use */
+  PSTEP_REFERENCE_SUMS = 4   /* with TRACK_ORDER: add every deposit in the reference's particle
+                                order, so deposited fields are bit-identical to the reference
+                                (slower; without it the order is fixed but different) */
 };
 
 /* Scalars of params.h that the particle step reads (params.cpp:22-56). The

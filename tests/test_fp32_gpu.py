@@ -1,0 +1,103 @@
+"""The FP32 mixed form against the FP64 oracle.
+
+Bound (uncorrected FP32 step vs the FP64 oracle): relative error <= 1e-5,
+measured norm-wise per quantity as max|fp32 - fp64| / max|fp64| (positions as
+max|dx| / L), after every step. The concentration's ghost layer is excluded:
+the reference leaves unfolded partial sums there (no refresh), the FP32 form
+periodic copies. Deposits are exact 64-bit fixed-point sums, so two runs are
+bit-identical.
+"""
+import numpy as np
+import pytest
+
+import helpers
+import pyoracle
+from first_repo_gb300 import gen, pstep
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5
+FIELDS = ["C", "Ax", "Ay", "Az", "E"]
+
+
+def run_pair(name, steps=None):
+    cdef = helpers.golden_case(name)
+    steps = steps or cdef["steps"]
+    case = gen.make_case(cdef["n"], cdef["count"], cdef["seed"], cdef["clustered"])
+    bp = helpers.make_bp(cdef["n"], cdef["count"], cdef.get("extra"))
+    cfg = bp.step_config()
+    arrs = [np.ascontiguousarray(case[k]) for k in ("x", "y", "z", "u", "v", "w", "t", "flag")]
+    ux, uy, uz, tf = helpers.ghosted_fields(case)
+    o = pyoracle.Oracle(cfg, cdef["count"])
+    o.load(*arrs)
+    g = pstep.ParticleStep(cfg, cdef["count"], pstep.FP32, 0)
+    g.load(*arrs)
+    g.bind_velocity(ux, uy, uz)
+    g.bind_temperature(tf)
+    o.prime(tf)
+    g.prime()
+    errs = []
+    for _ in range(steps):
+        o.run(1, ux, uy, uz, tf)
+        g.run(1)
+        errs.append(compare(o, g, bp.l))
+    return errs, g
+
+
+def compare(o, g, L):
+    fo, fg = o.flag(), g.array("flag")
+    io, ig = np.argsort(fo), np.argsort(fg)
+    assert np.array_equal(fo[io], fg[ig])
+    out = {}
+    for k in ("x", "y", "z"):
+        d = g.array(k)[ig] - o.array(k)[io]
+        d = (d + L / 2) % L - L / 2  # periodic images
+        out[k] = float(np.max(np.abs(d)) / L)
+    for k in ("u", "v", "w", "T", "RHS_T"):
+        a, b = g.array(k)[ig], o.array(k)[io]
+        out[k] = helpers.max_rel_to_max(a, b)
+    for f in FIELDS:
+        a, b = g.field(helpers.FIELD_MAP[f]), o.fields[f]
+        if f == "C":
+            a, b = a[1:-1, 1:-1, 1:-1], b[1:-1, 1:-1, 1:-1]
+        out[f] = helpers.max_rel_to_max(a, b)
+    me, mo = g.energy_mean(), o.mean(o.fields["E"])
+    out["mean_E"] = abs(me - mo) / max(abs(mo), 1e-300)
+    return out
+
+
+@pytest.mark.parametrize("name", ["box16_twc_off_gravity", "box32_clustered", "box64_uniform"])
+def test_fp32_error_against_fp64_oracle(built_cuda, name):
+    errs, g = run_pair(name, steps=3)
+    for step, e in enumerate(errs):
+        bad = {k: v for k, v in e.items() if not v <= REL_TOL}
+        assert not bad, f"step {step}: {bad}"
+    rc, flags = g.check()
+    assert rc == 0, flags
+
+
+def test_fp32_deterministic(built_cuda):
+    cdef = helpers.golden_case("box32_clustered")
+    case = gen.make_case(cdef["n"], cdef["count"], cdef["seed"], cdef["clustered"])
+    bp = helpers.make_bp(cdef["n"], cdef["count"])
+    arrs = [np.ascontiguousarray(case[k]) for k in ("x", "y", "z", "u", "v", "w", "t", "flag")]
+    ux, uy, uz, tf = helpers.ghosted_fields(case)
+    outs = []
+    for _ in range(2):
+        g = pstep.ParticleStep(bp.step_config(), cdef["count"], pstep.FP32, 0)
+        g.load(*arrs)
+        g.bind_velocity(ux, uy, uz)
+        g.bind_temperature(tf)
+        g.prime()
+        g.run(2)
+        outs.append([g.field(helpers.FIELD_MAP[f]).copy() for f in FIELDS] + [g.array("x"), g.array("flag")])
+        g.close()
+    for a, b in zip(*outs):
+        assert helpers.bits_equal(a, b)
+
+
+def test_fp32_rejects_unsupported_grid(built_cuda):
+    bp = helpers.make_bp(12, 100)
+    with pytest.raises(pstep.PstepError) as e:
+        pstep.ParticleStep(bp.step_config(), 100, pstep.FP32, 0)
+    assert e.value.status == 2

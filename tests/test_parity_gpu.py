@@ -1,12 +1,13 @@
 """GPU parity: the FP64 drop-in through the C ABI against the oracle.
 
-With PSTEP_TRACK_ORDER the device path must reproduce the reference exactly:
-every particle array in the reference's order (the permutation Send_Recv
-leaves), the flags, and all five deposited fields including their ghost
-layers, bit for bit, at every call. The interior mean of RHS_Part_Temp is a
-different summation order (a fixed tree): relative tolerance 1e-12.
-Without order tracking, particle states match bit for bit by flag and the
-deposits to 1e-12 of the field's maximum (different, fixed summation order).
+With PSTEP_TRACK_ORDER | PSTEP_REFERENCE_SUMS the device path must reproduce
+the reference exactly: every particle array in the reference's order (the
+permutation Send_Recv leaves), the flags, and all five deposited fields
+including their ghost layers, bit for bit, at every call. The interior mean of
+RHS_Part_Temp is a different summation order (a fixed tree): relative
+tolerance 1e-12. With the fast deposit (no REFERENCE_SUMS) particle states and
+order stay bit-exact and the deposits match to 1e-12 of the field's maximum
+(a different, fixed summation order).
 """
 import numpy as np
 import pytest
@@ -22,7 +23,10 @@ MEAN_RTOL = 1e-12
 DEPOSIT_TOL = 1e-12  # max|gpu - oracle| / max|oracle| without order tracking
 
 
-def setup_pair(cdef, flags=pstep.TRACK_ORDER):
+EXACT = pstep.TRACK_ORDER | pstep.REFERENCE_SUMS
+
+
+def setup_pair(cdef, flags=EXACT):
     case = gen.make_case(cdef["n"], cdef["count"], cdef["seed"], cdef["clustered"])
     bp = helpers.make_bp(cdef["n"], cdef["count"], cdef.get("extra"))
     cfg = bp.step_config()
@@ -36,14 +40,17 @@ def setup_pair(cdef, flags=pstep.TRACK_ORDER):
     return case, o, g, fields
 
 
-def compare_exact(o, g, where):
+def compare_exact(o, g, where, exact_fields=True):
     for name in helpers.PART:
         a, b = g.array(name), o.array(name)
         assert helpers.bits_equal(a, b), f"{where}: {name} differs (max abs {np.max(np.abs(a - b))})"
     assert np.array_equal(g.array("flag"), o.flag()), f"{where}: particle order differs"
     for f in FIELDS:
         a, b = g.field(helpers.FIELD_MAP[f]), o.fields[f]
-        assert helpers.bits_equal(a, b), f"{where}: field {f} differs (max rel {helpers.max_rel_to_max(a, b):.3e})"
+        if exact_fields:
+            assert helpers.bits_equal(a, b), f"{where}: field {f} differs (max rel {helpers.max_rel_to_max(a, b):.3e})"
+        else:
+            assert helpers.max_rel_to_max(a, b) <= DEPOSIT_TOL, f"{where}: field {f} {helpers.max_rel_to_max(a, b):.3e}"
     me, mo = g.energy_mean(), o.mean(o.fields["E"])
     assert abs(me - mo) <= MEAN_RTOL * max(abs(mo), 1e-300), f"{where}: energy mean {me} vs {mo}"
 
@@ -67,6 +74,25 @@ def test_fp64_bit_exact_in_reference_order(built_cuda, name):
     compare_exact(o, g, "end")
     rc, flags = g.check()
     assert rc == 0 and flags == 0
+
+
+@pytest.mark.parametrize("name", ["box16_twc_off_gravity", "box32_clustered", "box64_uniform"])
+def test_fp64_fast_deposit_reference_order(built_cuda, name):
+    """Default drop-in mode: bit-exact states and order, deposits to 1e-12 of max."""
+    cdef = helpers.golden_case(name)
+    _, o, g, (ux, uy, uz, tf) = setup_pair(cdef, flags=pstep.TRACK_ORDER)
+    o.prime(tf)
+    g.prime()
+    compare_exact(o, g, "prime", exact_fields=False)
+    for s in range(cdef["steps"]):
+        for k in range(4):
+            o.stage(k, ux, uy, uz, tf)
+            g.stage(k)
+            compare_exact(o, g, f"step {s} stage {k}", exact_fields=False)
+            o.end_stage()
+            g.end_stage()
+        o.end_step()
+        g.end_step()
 
 
 def test_fp64_split_calls_and_late_temperature(built_cuda):
