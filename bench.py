@@ -50,6 +50,21 @@ FP64_ADVANCE_CELL_BYTES = 4 * 8
 #   k=1..3 read base, *_int, *_np1 + RHS_T = 100 B; write 80 B.  fp32 fields U(3), T once per launch.
 FP32_ADVANCE_BYTES = {0: 36 + 80, 1: 100 + 80, 2: 100 + 80, 3: 100 + 80}
 FP32_ADVANCE_CELL_BYTES = 4 * 4
+# Deposits, per particle and per cell of one launch:
+#   FP32 (one fused walk): *_int cell+offsets (16) + RHS_u (12) + *_new cell+offsets (16) + RHS_T (4) = 48 B;
+#        per cell: cell_start (4) + five fp64 fields written (40) = 44 B.
+#   FP64 int deposit: x_int record (3 frac + key = 28) + RHS_u (24) = 52 B; per cell: cell_start (4) +
+#        four fp64 fields written (32) = 36 B.   FP64 temperature deposit: x_new record (28) + RHS_T (8) = 36 B;
+#        per cell: cell_start (4) + one field (8) = 12 B.
+#   FP64 counting sort: key read twice + index written (12 B); per cell: counts/scan/cursor (~20 B).
+PHASE_BYTES = {
+    ("fp32", "advance"): (sum(FP32_ADVANCE_BYTES.values()) / 4.0, FP32_ADVANCE_CELL_BYTES),
+    ("fp32", "deposit_int"): (48.0, 44.0),
+    ("fp64", "advance"): (sum(FP64_ADVANCE_BYTES.values()) / 4.0, FP64_ADVANCE_CELL_BYTES),
+    ("fp64", "deposit_int"): (52.0, 36.0),
+    ("fp64", "deposit_temp"): (36.0, 12.0),
+    ("fp64", "sort"): (12.0, 20.0),
+}
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
@@ -207,7 +222,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="box512_clustered", choices=sorted(config.WORKLOADS))
-    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--no-fp64-line", action="store_true", help="skip timing the FP64 drop-in beside the FP32 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -266,24 +282,24 @@ def main():
     ms_per_step = ms / args.steps
     value = world * n / (ms_per_step / 1e3)
 
-    # roofline of the dominant phase
+    # roofline of the dominant phase (live CUDA-event time of its launches in the timed region)
     peak, peak_kind = peaks()
     dom = max(prof, key=lambda p: prof[p][0])
     dom_ms, dom_cnt = prof[dom]
     roof = None
-    if dom == "advance" and dom_cnt:
-        pb, cb = (FP32_ADVANCE_BYTES, FP32_ADVANCE_CELL_BYTES) if form == pstep.FP32 else \
-            (FP64_ADVANCE_BYTES, FP64_ADVANCE_CELL_BYTES)
-        per_launch = n * sum(pb.values()) / 4.0 + cb * (wl.n + 2) ** 3
+    model = PHASE_BYTES.get((args.form, dom))
+    if model and dom_cnt:
+        per_launch = n * model[0] + model[1] * (wl.n + 2) ** 3
         achieved = per_launch / (dom_ms / dom_cnt / 1e3) / 1e9
         traffic = None
         tf_path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
         if os.path.exists(tf_path):
             with open(tf_path) as f:
-                traffic = json.load(f).get(f"{args.form}_advance_{wl.name}")
-        roof = {"kernel": "k_advance", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                traffic = json.load(f).get(f"{args.form}_{dom}_{wl.name}")
+        roof = {"kernel_phase": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": per_launch, "mean_launch_ms": dom_ms / dom_cnt}
+                "algorithmic_bytes_per_launch": per_launch, "mean_launch_ms": dom_ms / dom_cnt,
+                "launches": dom_cnt}
     phases = {p: {"ms_per_step": v[0] / args.steps, "launch_groups": v[1]} for p, v in prof.items()}
 
     # end to end through the C ABI with host buffers (pinned)
@@ -322,6 +338,23 @@ def main():
                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3}
         del C
 
+    # the FP64 drop-in on the same inputs, timed the same way (the comparison the metric names)
+    fp64 = None
+    if form == pstep.FP32 and not args.no_fp64_line:
+        g.close()
+        g64 = pstep.ParticleStep(bp.step_config(), n, pstep.FP64, pstep.TRACK_ORDER)
+        g64.load(*arrs)
+        g64.bind_velocity(*fields[:3])
+        g64.bind_temperature(fields[3])
+        g64.prime()
+        for _ in range(args.warmup):
+            g64.run(1)
+        barrier()
+        g64.run(args.steps)
+        ms64 = g64.last_run_ms() / args.steps
+        fp64 = {"value": world * n / (ms64 / 1e3), "ms_per_step": ms64, "form": "fp64 drop-in (reference order)"}
+        g = g64
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, dt = cpu_sample_rate()
@@ -339,7 +372,8 @@ def main():
                        "order_tracking": bool(flags & pstep.TRACK_ORDER), "clustered": wl.clustered,
                        "l2": "inputs larger than L2 (particle state alone is several GB)",
                        "parallelism": f"replicas x{world}", "input_generation_s": round(gen_s, 2)},
-            "roofline": roof, "phases": phases, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "roofline": roof, "phases": phases, "fp64_dropin": fp64, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches,
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -361,11 +361,13 @@ __global__ void k_refresh_z(Geom G, FieldSet fs) {
 constexpr int kRedBlocks = 1024;
 __global__ void k_sum_partial(Geom G, const double *__restrict__ f, double *__restrict__ part) {
   __shared__ double sm[kThreads];
-  const long long n3 = (long long)G.n[0] * G.n[1] * G.n[2];
+  // rows (j,k) distributed over blocks, the i loop over threads: fixed order, coalesced
+  const long long rows = (long long)G.n[1] * G.n[2];
   double s = 0.0;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n3; c += (long long)gridDim.x * blockDim.x) {
-    int i = (int)(c % G.n[0]) + 1, j = (int)((c / G.n[0]) % G.n[1]) + 1, k = (int)(c / ((long long)G.n[0] * G.n[1])) + 1;
-    s += f[glin(G, i, j, k)];
+  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int j = (int)(r % G.n[1]) + 1, k = (int)(r / G.n[1]) + 1;
+    const double *row = f + glin(G, 0, j, k);
+    for (int i = threadIdx.x + 1; i <= G.n[0]; i += blockDim.x) s += row[i];
   }
   sm[threadIdx.x] = s;
   __syncthreads();

@@ -263,7 +263,7 @@ int64_t scan_blocks_needed(int64_t n) { return (n + kScanTile - 1) / kScanTile; 
 // Counting sort of the h->np particles by (keys[i] >> shift) into nkeys buckets:
 // cell_start[0..nkeys] and sidx, every bucket ordered by the secondary key.
 int csr_sort(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, const int32_t *order, int32_t *cell_start,
-             int32_t *sidx) {
+             int32_t *sidx, int order_within) {
   PSTEP_CUDA(cudaMemsetAsync(h->counts, 0, sizeof(int32_t) * nkeys, h->stream));
   if (h->np > 0) {
     k_count<<<blocks_for(h->np), kThreads, 0, h->stream>>>(keys, shift, h->np, h->counts);
@@ -274,6 +274,7 @@ int csr_sort(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, const
   if (h->np > 0) {
     k_scatter<<<blocks_for(h->np), kThreads, 0, h->stream>>>(keys, shift, h->np, h->cursor, sidx);
     PSTEP_LAUNCHED(h);
+    if (!order_within) return PSTEP_OK;
     PSTEP_CUDA(cudaMemsetAsync(h->big_count, 0, sizeof(int32_t), h->stream));
     k_segsort_small<<<blocks_for(nkeys), kThreads, 0, h->stream>>>(cell_start, nkeys, sidx, order, keys, h->big_list,
                                                                     h->big_count, h->err_word);
@@ -289,7 +290,7 @@ int csr_sort(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, const
 int sort_by_node(pstep_ctx *h, const uint32_t *keys, Csr &out) {
   const int32_t *order =
       ((h->cfg.flags & PSTEP_TRACK_ORDER) && (h->cfg.flags & PSTEP_REFERENCE_SUMS)) ? h->ref_of_phys : nullptr;
-  int rc = csr_sort(h, keys, 3, h->geom.gsize, order, out.cell_start, out.sidx);
+  int rc = csr_sort(h, keys, 3, h->geom.gsize, order, out.cell_start, out.sidx, 1);
   out.identity = 0;
   return rc;
 }

@@ -47,11 +47,32 @@ constexpr int kHalo = 2;          // source cells beyond the brick
 constexpr int kSrc = kBr + 2 * kHalo;
 constexpr int kDepThreads = 256;
 constexpr int kMaxN = 1024;       // 10 bits per cell coordinate
+constexpr int kBoundSlots = 1024;
 
 struct Set32 {
   uint32_t *cell;
   float *o[3];
   float *v[4];  // u v w T
+};
+
+// Work list of the deposit: one item per brick, or -- for bricks holding more
+// than kSplitMin particles -- several items, each a slice of the brick's source
+// particles. Items of split bricks come first (largest work first), then the
+// rest; CTAs take items in order from an atomic counter.
+constexpr int kChunkVisits = 32768;   // target particle visits per item
+constexpr int kSplitMin = kChunkVisits / 4;
+constexpr int kMaxChunks = 256;
+
+struct Work {
+  int32_t *items;       // (brick << 8) | chunk
+  int32_t *nchunk;      // per brick
+  int32_t *slot;        // per brick: index of its global tile, or -1
+  int32_t *cnt_a, *cnt_b, *cnt_s, *off_a, *off_b, *off_s;  // per brick (+1) scan arrays
+  int32_t *n_items;     // device scalar
+  int32_t *next;        // device counters, one per deposit launch
+  int32_t *done;        // per slot: items finished
+  long long *tiles;     // per slot: 5 x 512 int64
+  int64_t slot_cap;
 };
 
 struct F32Form {
@@ -65,7 +86,10 @@ struct F32Form {
   int32_t *sidx;
   float *tmpf;        // permutation scratch
   uint32_t *bounds;   // [0..2] max |RHS_u| per component (float bits), [3] max |RHS_T|, [4] max per-cell count
+  uint32_t *slots;    // kBoundSlots x 4 partial maxima (spread so blocks do not contend on one word)
   int32_t *se;        // fixed-point scale exponents per field
+  Work work;
+  int launch_no;      // deposit launches since the last work-list build (counter index)
   int sorted;
   int tref_set;
   double tref;        // temperature reference (see above)
@@ -105,6 +129,26 @@ __device__ inline long long glin3(const Geom &G, int i, int j, int k) { return g
 __device__ inline void atomic_max_abs(uint32_t *w, float v) {
   // non-negative floats order like their bit patterns
   atomicMax(w, __float_as_uint(fabsf(v)));
+}
+
+// block maximum of 4 non-negative values into slot blockIdx % kBoundSlots
+__device__ inline void block_max4(uint32_t *slots, float a0, float a1, float a2, float a3) {
+  __shared__ float red[4][32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 = fmaxf(a0, __shfl_xor_sync(0xffffffffu, a0, o));
+    a1 = fmaxf(a1, __shfl_xor_sync(0xffffffffu, a1, o));
+    a2 = fmaxf(a2, __shfl_xor_sync(0xffffffffu, a2, o));
+    a3 = fmaxf(a3, __shfl_xor_sync(0xffffffffu, a3, o));
+  }
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0) { red[0][w] = a0; red[1][w] = a1; red[2][w] = a2; red[3][w] = a3; }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    float m = 0.f;
+    for (int q = 0; q < nw; ++q) m = fmaxf(m, red[threadIdx.x][q]);
+    atomic_max_abs(&slots[(blockIdx.x % kBoundSlots) * 4 + threadIdx.x], m);
+  }
 }
 
 struct C32 {
@@ -203,20 +247,7 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
     mu0 = rhs[0]; mu1 = rhs[1]; mu2 = rhs[2]; mt = rhs_t_new;
   }
   // bounds for the fixed-point scales (order-independent maxima)
-  float a0 = fabsf(mu0), a1 = fabsf(mu1), a2 = fabsf(mu2), a3 = fabsf(mt);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a0 = fmaxf(a0, __shfl_xor_sync(0xffffffffu, a0, o));
-    a1 = fmaxf(a1, __shfl_xor_sync(0xffffffffu, a1, o));
-    a2 = fmaxf(a2, __shfl_xor_sync(0xffffffffu, a2, o));
-    a3 = fmaxf(a3, __shfl_xor_sync(0xffffffffu, a3, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomic_max_abs(&f.bounds[0], a0);
-    atomic_max_abs(&f.bounds[1], a1);
-    atomic_max_abs(&f.bounds[2], a2);
-    atomic_max_abs(&f.bounds[3], a3);
-  }
+  block_max4(f.slots, fabsf(mu0), fabsf(mu1), fabsf(mu2), fabsf(mt));
 }
 
 // the prime (grid.cpp:223-226) at the base positions: Tg, RHS_T
@@ -240,35 +271,51 @@ __global__ void k_prime32(Geom G, F32Form f, float itth, int64_t n) {
     mt = (tg - B.v[3][p]) * itth;
     f.rhs_t[p] = mt;
   }
-  float a3 = fabsf(mt);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) a3 = fmaxf(a3, __shfl_xor_sync(0xffffffffu, a3, o));
-  if ((threadIdx.x & 31) == 0) atomic_max_abs(&f.bounds[3], a3);
+  block_max4(f.slots, 0.f, 0.f, 0.f, fabsf(mt));
 }
 
-// exponents of the fixed-point scales: max|sum| <= bound = max|contribution| * 8 * 27 * max count per cell
+// exponents of the fixed-point scales
 __global__ void k_scales(F32Form f) {
+  // fold the spread partial maxima, then clear them for the next stage
+  for (int q = 0; q < 4; ++q) {
+    uint32_t m = 0;
+    for (int s = threadIdx.x; s < kBoundSlots; s += blockDim.x) m = max(m, f.slots[s * 4 + q]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) f.bounds[q] = m;
+  }
+  __syncwarp();
+  for (int s = threadIdx.x; s < kBoundSlots * 4; s += blockDim.x) f.slots[s] = 0;
   if (threadIdx.x != 0) return;
-  const float cnt = 8.f * 27.f * fmaxf(1.f, (float)f.bounds[4]);
-  const float b[5] = {cnt, __uint_as_float(f.bounds[0]) * cnt, __uint_as_float(f.bounds[1]) * cnt,
-                      __uint_as_float(f.bounds[2]) * cnt, __uint_as_float(f.bounds[3]) * cnt};
+  // largest contribution of each field: concentration weights <= 1, momentum |RHS_u|,
+  // energy |RHS_T| (weights <= 1); its magnitude maps to at most 2^24
+  const float b[5] = {1.f, __uint_as_float(f.bounds[0]), __uint_as_float(f.bounds[1]), __uint_as_float(f.bounds[2]),
+                      __uint_as_float(f.bounds[3])};
   for (int q = 0; q < 5; ++q) {
     int e = 0;
     if (b[q] > 0.f && isfinite(b[q])) frexpf(b[q], &e);  // b < 2^e
-    int se = 61 - e;
+    int se = 24 - e;
     if (se > 100) se = 100;
     f.se[q] = se;
   }
 }
 
-// max particles per cell of the step sort (bound for the scales)
+// max particles per cell of the step sort (bound for the scales): grid-stride, one
+// atomic per block
 __global__ void k_max_count(const int32_t *__restrict__ cs, int64_t ncell, uint32_t *__restrict__ out) {
-  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ uint32_t red[32];
   uint32_t m = 0;
-  if (c < ncell) m = (uint32_t)(cs[c + 1] - cs[c]);
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, (uint32_t)(cs[c + 1] - cs[c]));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < (int)(blockDim.x >> 5); ++q) m = max(m, red[q]);
+    m = max(m, red[0]);
+    if (m) atomicMax(out, m);
+  }
 }
 
 // exact conversion of a scaled 64-bit integer sum q * 2^-se to fp64 with integer operations
@@ -289,147 +336,290 @@ __device__ inline double fixed_to_f64(long long q, int se) {
   return __longlong_as_double((long long)((sgn << 63) | ((unsigned long long)ex << 52) | man));
 }
 
-__device__ inline long long to_fixed(float v, int se) { return __float2ll_rn(ldexpf(v, se)); }
+// c - b taken periodically into (-n/2, n/2]
+__device__ inline int rel_local(int c, int b, int n) {
+  int r = c - b;
+  const int half = n >> 1;
+  r += (r <= -half) ? n : 0;
+  r -= (r > half) ? n : 0;
+  return r;
+}
 
-// Warp-cooperative exact add into shared int64 accumulators: lanes with the same
-// slot (slot < 0: nothing to add) are summed first, in three 21-bit pieces whose
-// sums over 32 lanes cannot overflow, and the group's lowest lane adds once.
-// Must be called by all 32 lanes.
-__device__ inline void warp_add_fixed(long long *acc, int slot, long long v) {
-  const unsigned peers = __match_any_sync(0xffffffffu, slot);
-  if (slot < 0) return;
+// Exact sums with 32-bit shared-memory atomics. Every contribution is scaled so
+// that the largest magnitude is 2^24 (the fp32 values carry 24 significant bits,
+// so nothing beyond their own rounding is lost) and rounded to a 64-bit integer
+// of magnitude below 2^25. A slot holds the two's-complement sum in two 32-bit
+// words: the low word is added with its old value returned, and the high word
+// changes only on a carry or borrow out of the low word (rare at this size:
+// about once per 2^7 or more adds). The pair is the exact sum modulo 2^64,
+// whatever the order of the adds.
+__device__ inline void add_fixed(uint32_t *lo, uint32_t *hi, long long v) {
   const unsigned long long u = (unsigned long long)v;
-  const unsigned lo = (unsigned)(u & 0x1fffffu);
-  const unsigned mid = (unsigned)((u >> 21) & 0x1fffffu);
-  const int hi = (int)(v >> 42);  // arithmetic shift: signed top part
-  const unsigned slo = __reduce_add_sync(peers, lo);
-  const unsigned smid = __reduce_add_sync(peers, mid);
-  const int shi = (int)__reduce_add_sync(peers, (unsigned)hi);
-  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
-    const long long sum = ((long long)shi << 42) + ((long long)smid << 21) + (long long)slo;
-    atomicAdd((unsigned long long *)&acc[slot], (unsigned long long)sum);
+  const uint32_t vl = (uint32_t)u;
+  const uint32_t vh = (uint32_t)(u >> 32);
+  const uint32_t old = atomicAdd(lo, vl);
+  const uint32_t carry = (uint32_t)(old + vl) < old ? 1u : 0u;
+  if (vh + carry) atomicAdd(hi, vh + carry);
+}
+__device__ inline long long get_fixed(const uint32_t *lo, const uint32_t *hi) {
+  return (long long)(((unsigned long long)*hi << 32) | (unsigned long long)*lo);
+}
+
+// accumulator slot of brick-local cell (x,y,z): rows padded by one word so that
+// neighbouring rows do not fall on the same shared-memory banks
+constexpr int kRow = kBr + 1;
+constexpr int kAccSlots = kRow * kBr * kBr;
+__device__ inline int slot_of(int x, int y, int z) { return (z * kBr + y) * kRow + x; }
+
+__global__ void k_work_count(Geom G, const int32_t *__restrict__ cs, Work w, int nb) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const int32_t nbp = cs[(int64_t)(b + 1) * kBr * kBr * kBr] - cs[(int64_t)b * kBr * kBr * kBr];
+  int c = 1;
+  if (nbp > kSplitMin) c = min(kMaxChunks, (int)((4ll * nbp + kChunkVisits - 1) / kChunkVisits));
+  const bool split = c > 1;
+  w.cnt_a[b] = split ? c : 0;
+  w.cnt_b[b] = split ? 0 : 1;
+  w.cnt_s[b] = split ? 1 : 0;
+  w.nchunk[b] = c;
+}
+
+__global__ void k_work_fill(Work w, int nb) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t total_a = w.off_a[nb];
+  if (b == 0) *w.n_items = total_a + w.off_b[nb];
+  if (b >= nb) return;
+  const int c = w.nchunk[b];
+  if (c > 1 && w.off_s[b] < w.slot_cap) {
+    w.slot[b] = w.off_s[b];
+    for (int q = 0; q < c; ++q) w.items[w.off_a[b] + q] = (b << 8) | q;
+  } else {
+    if (c > 1) {  // no tile left: run the brick as one item (slower, same result)
+      w.nchunk[b] = 1;
+      for (int q = 1; q < c; ++q) w.items[w.off_a[b] + q] = -1;
+      w.items[w.off_a[b]] = (b << 8);
+    } else {
+      w.items[total_a + w.off_b[b]] = (b << 8);
+    }
+    w.slot[b] = -1;
   }
 }
 
-// Deposit into the CTA's brick of 8^3 interior cells. mode 0: concentration + face
-// momentum at the *_int positions; mode 1: RHS_T at the *_new positions.
-template <int MODE>
-__global__ void __launch_bounds__(kDepThreads) k_dep32(Geom G, F32Form f, Set32 S, int twc, double *__restrict__ out0,
-                                                       double *__restrict__ ox_, double *__restrict__ oy_,
-                                                       double *__restrict__ oz_) {
-  constexpr int NF = MODE == 0 ? 4 : 1;
-  __shared__ long long acc[NF][kBr * kBr * kBr];
-  __shared__ int32_t pre[kSrc * kSrc * kSrc + 1];
-  __shared__ int32_t beg[kSrc * kSrc * kSrc];
-  const int nbx = G.n[0] / kBr, nby = G.n[1] / kBr;
-  const int bx = (int)(blockIdx.x % nbx) * kBr;
-  const int by = (int)((blockIdx.x / nbx) % nby) * kBr;
-  const int bz = (int)(blockIdx.x / (nbx * nby)) * kBr;
-  for (int s = threadIdx.x; s < NF * kBr * kBr * kBr; s += blockDim.x) (&acc[0][0])[s] = 0;
-  // source cells [b-2, b+B+2): counts -> exclusive prefix (flat particle index space)
+// Deposit into bricks of 8^3 interior cells, one walk over each brick's source
+// particles per stage: at the *_int positions the concentration and the face
+// momentum (DO_INT), at the *_new positions RHS_T (DO_NEW). Field slots:
+// 0 C, 1-3 RHS_RU x/y/z, 4 RHS_Part_Temp (scale exponents f.se[0..4]).
+template <bool DO_INT, bool DO_NEW>
+__global__ void __launch_bounds__(kDepThreads) k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w, int twc,
+                                                       double *__restrict__ outC, double *__restrict__ outX,
+                                                       double *__restrict__ outY, double *__restrict__ outZ,
+                                                       double *__restrict__ outE) {
+  constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
+  constexpr int FE = DO_INT ? 4 : 0;  // accumulator index of RHS_Part_Temp
   constexpr int NS = kSrc * kSrc * kSrc;
-  for (int s = threadIdx.x; s < NS; s += blockDim.x) {
-    const int lx = s % kSrc, ly = (s / kSrc) % kSrc, lz = s / (kSrc * kSrc);
-    const int i = wrapi(bx - kHalo + lx, G.n[0]), j = wrapi(by - kHalo + ly, G.n[1]), k = wrapi(bz - kHalo + lz, G.n[2]);
-    const uint32_t id = brick_id(G, i, j, k);
-    const int32_t a = f.cell_start[id], e = f.cell_start[id + 1];
-    beg[s] = a;
-    pre[s + 1] = e - a;
-  }
-  if (threadIdx.x == 0) pre[0] = 0;
-  __syncthreads();
-  // sequential-by-warp prefix over NS entries (small)
-  if (threadIdx.x < 32) {
-    int32_t carry = 0;
-    for (int base = 0; base < NS; base += 32) {
-      int idx = base + threadIdx.x + 1;
-      int32_t v = idx <= NS ? pre[idx] : 0;
+  constexpr int NB3 = kBr * kBr * kBr;
+  __shared__ uint32_t acc_lo[NF][kAccSlots];
+  __shared__ uint32_t acc_hi[NF][kAccSlots];
+  __shared__ int32_t pre[NS + 1];
+  __shared__ int32_t beg[NS];
+  __shared__ int32_t sh_item, sh_last;
+  const int nbx = G.n[0] / kBr, nby = G.n[1] / kBr;
+  const int32_t n_items = *w.n_items;
+  float scale[5];
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int32_t y = __shfl_up_sync(0xffffffffu, v, o);
-        if ((int)threadIdx.x >= o) v += y;
-      }
-      if (idx <= NS) pre[idx] = v + carry;
-      carry += __shfl_sync(0xffffffffu, v, 31);
-    }
-  }
-  __syncthreads();
-  const int32_t total = pre[NS];
-  int se[4];
-#pragma unroll
-  for (int q = 0; q < NF; ++q) se[q] = f.se[MODE == 0 ? q : 4];
-  // every lane runs the same number of iterations (the adds are warp-cooperative)
-  const int32_t rounds = (total + (int32_t)blockDim.x - 1) / (int32_t)blockDim.x;
-  for (int32_t it = 0; it < rounds; ++it) {
-    const int32_t t = it * (int32_t)blockDim.x + (int32_t)threadIdx.x;
-    const bool live = t < total;
-    // find the source cell: last s with pre[s] <= t
-    int lo = 0, hi = NS;
-    while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (pre[mid] <= t) lo = mid; else hi = mid;
-    }
-    const int32_t p = live ? beg[lo] + (t - pre[lo]) : 0;  // dead lanes read particle 0 (total > 0 here)
-    const uint32_t c = S.cell[p];
-    const float o0 = S.o[0][p], o1 = S.o[1][p], o2 = S.o[2][p];
-    const int c3[3] = {ci_(c), cj_(c), ck_(c)};
+  for (int q = 0; q < 5; ++q) scale[q] = ldexpf(1.0f, f.se[q]);  // exact powers of two
+  while (true) {
+    if (threadIdx.x == 0) sh_item = atomicAdd(&w.next[0], 1);
+    __syncthreads();
+    const int32_t item_idx = sh_item;
+    if (item_idx >= n_items) break;
+    const int32_t item = w.items[item_idx];
+    if (item < 0) { __syncthreads(); continue; }
+    const int brick = item >> 8, chunk = item & 255;
+    const int nch = w.nchunk[brick];
+    const int bx = (brick % nbx) * kBr, by = ((brick / nbx) % nby) * kBr, bz = (brick / (nbx * nby)) * kBr;
     const int b3[3] = {bx, by, bz};
-    // trilinear: node = cell + h; targets node - o (periodic); factor o ? 1 - x_l : x_l
-    const int h3[3] = {o0 >= 0.5f, o1 >= 0.5f, o2 >= 0.5f};
-    const float xl3[3] = {o0 - h3[0] + 0.5f, o1 - h3[1] + 0.5f, o2 - h3[2] + 0.5f};
-    int lt[3][2];  // local brick coordinate of target node - o, or -1
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int o = 0; o < 2; ++o) {
-        int tt = wrapi(c3[d] + h3[d] - o, G.n[d]) - b3[d];
-        lt[d][o] = (tt >= 0 && tt < kBr) ? tt : -1;
-      }
-    const float val = MODE == 0 ? 1.0f : f.rhs_t[p];
-#pragma unroll
-    for (int o = 0; o < 8; ++o) {
-      const int ox = (o >> 2) & 1, oy = (o >> 1) & 1, oz = o & 1;
-      const bool in = live && lt[0][ox] >= 0 && lt[1][oy] >= 0 && lt[2][oz] >= 0;
-      const float w = (ox ? 1.f - xl3[0] : xl3[0]) * (oy ? 1.f - xl3[1] : xl3[1]) * (oz ? 1.f - xl3[2] : xl3[2]) * val;
-      const int slot = in ? (lt[2][oz] * kBr + lt[1][oy]) * kBr + lt[0][ox] : -1;
-      warp_add_fixed(acc[0], slot, in ? to_fixed(w, se[0]) : 0ll);
+    for (int s = threadIdx.x; s < NF * kAccSlots; s += blockDim.x) {
+      (&acc_lo[0][0])[s] = 0u;
+      (&acc_hi[0][0])[s] = 0u;
     }
-    if (MODE == 0 && twc) {
-      // face-normal (particle.cpp:498-524): face c gets (1 - x_l) R, face c + 1 gets x_l R
+    // source cells [b-2, b+B+2): counts -> exclusive prefix (flat particle index space)
+    for (int s = threadIdx.x; s < NS; s += blockDim.x) {
+      const int lx = s % kSrc, ly = (s / kSrc) % kSrc, lz = s / (kSrc * kSrc);
+      int i = bx - kHalo + lx, j = by - kHalo + ly, k = bz - kHalo + lz;
+      i += i < 0 ? G.n[0] : 0; i -= i >= G.n[0] ? G.n[0] : 0;
+      j += j < 0 ? G.n[1] : 0; j -= j >= G.n[1] ? G.n[1] : 0;
+      k += k < 0 ? G.n[2] : 0; k -= k >= G.n[2] ? G.n[2] : 0;
+      const uint32_t id = brick_id(G, i, j, k);
+      const int32_t a0 = f.cell_start[id], e0 = f.cell_start[id + 1];
+      beg[s] = a0;
+      pre[s + 1] = e0 - a0;
+    }
+    if (threadIdx.x == 0) pre[0] = 0;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      int32_t carry = 0;
+      for (int base = 0; base < NS; base += 32) {
+        int idx = base + threadIdx.x + 1;
+        int32_t v = idx <= NS ? pre[idx] : 0;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const int p1 = (d + 1) % 3, p2 = (d + 2) % 3;
-        const int a1 = c3[p1] - b3[p1], a2 = c3[p2] - b3[p2];
-        const bool across = live && a1 >= 0 && a1 < kBr && a2 >= 0 && a2 < kBr;
-        const float r = f.rhs_u[d][p];
-        const float xl = d == 0 ? o0 : (d == 1 ? o1 : o2);
+        for (int o = 1; o < 32; o <<= 1) {
+          int32_t y = __shfl_up_sync(0xffffffffu, v, o);
+          if ((int)threadIdx.x >= o) v += y;
+        }
+        if (idx <= NS) pre[idx] = v + carry;
+        carry += __shfl_sync(0xffffffffu, v, 31);
+      }
+    }
+    __syncthreads();
+    const int32_t total = pre[NS];
+    const int32_t t0 = (int32_t)(((int64_t)total * chunk) / nch);
+    const int32_t t1 = (int32_t)(((int64_t)total * (chunk + 1)) / nch);
+    for (int32_t t = t0 + (int32_t)threadIdx.x; t < t1; t += (int32_t)blockDim.x) {
+      // source cell: last s with pre[s] <= t
+      int lo = 0, hi = NS;
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (pre[mid] <= t) lo = mid; else hi = mid;
+      }
+      const int32_t p = beg[lo] + (t - pre[lo]);
+      if (DO_INT) {
+        const uint32_t c = SI.cell[p];
+        const int c3[3] = {ci_(c), cj_(c), ck_(c)};
+        int r3[3];
 #pragma unroll
-        for (int side = 0; side < 2; ++side) {
-          const int tt = wrapi(c3[d] + side, G.n[d]) - b3[d];
-          const bool in = across && tt >= 0 && tt < kBr;
-          int l3[3];
-          l3[d] = in ? tt : 0; l3[p1] = in ? a1 : 0; l3[p2] = in ? a2 : 0;
-          const float w = side ? xl * r : (1.f - xl) * r;
-          const int slot = in ? (l3[2] * kBr + l3[1]) * kBr + l3[0] : -1;
-          warp_add_fixed(acc[1 + d], slot, in ? to_fixed(w, se[1 + d]) : 0ll);
+        for (int d = 0; d < 3; ++d) r3[d] = rel_local(c3[d], b3[d], G.n[d]);
+        // reachable targets: trilinear cells r3 - 1 .. r3 + 1, faces r3 .. r3 + 1 (normal) and r3 (across)
+        const bool near = r3[0] >= -1 && r3[0] <= kBr && r3[1] >= -1 && r3[1] <= kBr && r3[2] >= -1 && r3[2] <= kBr;
+        if (near) {
+          const float o3[3] = {SI.o[0][p], SI.o[1][p], SI.o[2][p]};
+          // trilinear: node = cell + h, targets node - o, factor o ? 1 - x_l : x_l
+          int lt0[3];
+          float xl3[3];
+          bool any = true;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const int hh = o3[d] >= 0.5f;
+            xl3[d] = o3[d] - hh + 0.5f;
+            lt0[d] = r3[d] + hh;
+            any &= (lt0[d] >= 0) && (lt0[d] - 1 < kBr);
+          }
+          if (any) {
+#pragma unroll
+            for (int o = 0; o < 8; ++o) {
+              const int ox = (o >> 2) & 1, oy = (o >> 1) & 1, oz = o & 1;
+              const int tx = lt0[0] - ox, ty = lt0[1] - oy, tz = lt0[2] - oz;
+              if ((unsigned)tx >= (unsigned)kBr || (unsigned)ty >= (unsigned)kBr || (unsigned)tz >= (unsigned)kBr) continue;
+              const float wt = (ox ? 1.f - xl3[0] : xl3[0]) * (oy ? 1.f - xl3[1] : xl3[1]) * (oz ? 1.f - xl3[2] : xl3[2]);
+              const int sl = slot_of(tx, ty, tz);
+              add_fixed(&acc_lo[0][sl], &acc_hi[0][sl], __float2ll_rn(wt * scale[0]));
+            }
+          }
+          if (twc) {
+            // face-normal (particle.cpp:498-524): face c gets (1 - x_l) R, face c + 1 gets x_l R
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              const int p1 = (d + 1) % 3, p2 = (d + 2) % 3;
+              if ((unsigned)r3[p1] >= (unsigned)kBr || (unsigned)r3[p2] >= (unsigned)kBr) continue;
+              if (r3[d] < -1 || r3[d] >= kBr) continue;
+              const float r = f.rhs_u[d][p];
+              const float xl = o3[d];
+#pragma unroll
+              for (int side = 0; side < 2; ++side) {
+                const int tt = r3[d] + side;
+                if ((unsigned)tt >= (unsigned)kBr) continue;
+                int l3[3];
+                l3[d] = tt; l3[p1] = r3[p1]; l3[p2] = r3[p2];
+                const float wt = side ? xl * r : (1.f - xl) * r;
+                const int sl = slot_of(l3[0], l3[1], l3[2]);
+                add_fixed(&acc_lo[1 + d][sl], &acc_hi[1 + d][sl], __float2ll_rn(wt * scale[1 + d]));
+              }
+            }
+          }
+        }
+      }
+      if (DO_NEW) {
+        const uint32_t c = SN.cell[p];
+        const int c3[3] = {ci_(c), cj_(c), ck_(c)};
+        int r3[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) r3[d] = rel_local(c3[d], b3[d], G.n[d]);
+        const bool near = r3[0] >= -1 && r3[0] <= kBr && r3[1] >= -1 && r3[1] <= kBr && r3[2] >= -1 && r3[2] <= kBr;
+        if (near) {
+          const float o3[3] = {SN.o[0][p], SN.o[1][p], SN.o[2][p]};
+          int lt0[3];
+          float xl3[3];
+          bool any = true;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const int hh = o3[d] >= 0.5f;
+            xl3[d] = o3[d] - hh + 0.5f;
+            lt0[d] = r3[d] + hh;
+            any &= (lt0[d] >= 0) && (lt0[d] - 1 < kBr);
+          }
+          if (any) {
+            const float val = f.rhs_t[p];
+#pragma unroll
+            for (int o = 0; o < 8; ++o) {
+              const int ox = (o >> 2) & 1, oy = (o >> 1) & 1, oz = o & 1;
+              const int tx = lt0[0] - ox, ty = lt0[1] - oy, tz = lt0[2] - oz;
+              if ((unsigned)tx >= (unsigned)kBr || (unsigned)ty >= (unsigned)kBr || (unsigned)tz >= (unsigned)kBr) continue;
+              const float wt =
+                  (ox ? 1.f - xl3[0] : xl3[0]) * (oy ? 1.f - xl3[1] : xl3[1]) * (oz ? 1.f - xl3[2] : xl3[2]) * val;
+              const int sl = slot_of(tx, ty, tz);
+              add_fixed(&acc_lo[FE][sl], &acc_hi[FE][sl], __float2ll_rn(wt * scale[4]));
+            }
+          }
         }
       }
     }
-  }
-  __syncthreads();
-  for (int s = threadIdx.x; s < kBr * kBr * kBr; s += blockDim.x) {
-    const int lx = s % kBr, ly = (s / kBr) % kBr, lz = s / (kBr * kBr);
-    const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
-    out0[g] = fixed_to_f64(acc[0][s], se[0]);
-    if (MODE == 0) {
-      if (twc) {
-        ox_[g] = fixed_to_f64(acc[1][s], se[1]);
-        oy_[g] = fixed_to_f64(acc[2][s], se[2]);
-        oz_[g] = fixed_to_f64(acc[3][s], se[3]);
-      } else {
-        ox_[g] = 0.0; oy_[g] = 0.0; oz_[g] = 0.0;
+    __syncthreads();
+    const int slot = nch > 1 ? w.slot[brick] : -1;
+    if (slot >= 0) {
+      // split brick: add this slice into the brick's global tile; the last slice converts
+      long long *tile = w.tiles + (int64_t)slot * 5 * NB3;
+      for (int s = threadIdx.x; s < NF * NB3; s += blockDim.x) {
+        const int q = s / NB3, r = s % NB3;
+        const int sl = slot_of(r % kBr, (r / kBr) % kBr, r / (kBr * kBr));
+        const long long v = get_fixed(&acc_lo[q][sl], &acc_hi[q][sl]);
+        if (v) atomicAdd((unsigned long long *)&tile[s], (unsigned long long)v);
       }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) sh_last = (atomicAdd(&w.done[slot], 1) == nch - 1);
+      __syncthreads();
+      if (sh_last) {
+        __threadfence();
+        for (int s = threadIdx.x; s < NF * NB3; s += blockDim.x) {
+          const int q = s / NB3, r = s % NB3;
+          const int sl = slot_of(r % kBr, (r / kBr) % kBr, r / (kBr * kBr));
+          const unsigned long long v = (unsigned long long)__ldcg(&tile[s]);
+          acc_lo[q][sl] = (uint32_t)v;
+          acc_hi[q][sl] = (uint32_t)(v >> 32);
+          tile[s] = 0;  // ready for the next launch
+        }
+        if (threadIdx.x == 0) w.done[slot] = 0;
+      }
+      __syncthreads();
+      if (!sh_last) continue;
     }
+    for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
+      const int lx = s % kBr, ly = (s / kBr) % kBr, lz = s / (kBr * kBr);
+      const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
+      const int sl = slot_of(lx, ly, lz);
+      if (DO_INT) {
+        outC[g] = fixed_to_f64(get_fixed(&acc_lo[0][sl], &acc_hi[0][sl]), f.se[0]);
+        if (twc) {
+          outX[g] = fixed_to_f64(get_fixed(&acc_lo[1][sl], &acc_hi[1][sl]), f.se[1]);
+          outY[g] = fixed_to_f64(get_fixed(&acc_lo[2][sl], &acc_hi[2][sl]), f.se[2]);
+          outZ[g] = fixed_to_f64(get_fixed(&acc_lo[3][sl], &acc_hi[3][sl]), f.se[3]);
+        } else {
+          outX[g] = 0.0; outY[g] = 0.0; outZ[g] = 0.0;
+        }
+      }
+      if (DO_NEW) outE[g] = fixed_to_f64(get_fixed(&acc_lo[FE][sl], &acc_hi[FE][sl]), f.se[4]);
+    }
+    __syncthreads();
   }
 }
 
@@ -556,7 +746,7 @@ void dfree32(T *&p) {
     if (rc_ != PSTEP_OK) return rc_;   \
   } while (0)
 
-int dep_all(pstep_ctx *h, int mode);
+int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN);
 
 int sort_step(pstep_ctx *h) {
   // particles by brick-major cell of the base position; storage reordered; per-cell CSR kept
@@ -568,8 +758,9 @@ int sort_step(pstep_ctx *h) {
     k_keys32<<<nb(n), kThreads, 0, h->stream>>>(G, f.set[SBASE], n, f.key);
     PSTEP_LAUNCHED(h);
   }
-  // within a cell, by particle id (deterministic storage order)
-  TRY32(csr_sort(h, f.key, 0, ncell, h->s.flag, f.cell_start, f.sidx));
+  // The order inside a cell is left as the scatter makes it: every result of this form
+  // (integer deposit sums, per-particle states by id) is independent of storage order.
+  TRY32(csr_sort(h, f.key, 0, ncell, h->s.flag, f.cell_start, f.sidx, 0));
   if (n > 0) {
     Set32 &B = f.set[SBASE];
     auto permf = [&](float *&a) {
@@ -591,7 +782,18 @@ int sort_step(pstep_ctx *h) {
     h->launches += 9;
     PSTEP_LAUNCHED(h);
     PSTEP_CUDA(cudaMemsetAsync(&f.bounds[4], 0, sizeof(uint32_t), h->stream));
-    k_max_count<<<nb(ncell), kThreads, 0, h->stream>>>(f.cell_start, ncell, &f.bounds[4]);
+    k_max_count<<<1024, kThreads, 0, h->stream>>>(f.cell_start, ncell, &f.bounds[4]);
+    PSTEP_LAUNCHED(h);
+  }
+  {  // deposit work list for this step's particle distribution
+    Work &w = f.work;
+    const int nbk = (G.n[0] / kBr) * (G.n[1] / kBr) * (G.n[2] / kBr);
+    k_work_count<<<nb(nbk), kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+    PSTEP_LAUNCHED(h);
+    TRY32(exclusive_scan(h, w.cnt_a, nbk, w.off_a, nullptr));
+    TRY32(exclusive_scan(h, w.cnt_b, nbk, w.off_b, nullptr));
+    TRY32(exclusive_scan(h, w.cnt_s, nbk, w.off_s, nullptr));
+    k_work_fill<<<nb(nbk), kThreads, 0, h->stream>>>(w, nbk);
     PSTEP_LAUNCHED(h);
   }
   f.sorted = 1;
@@ -603,8 +805,9 @@ int sort_step(pstep_ctx *h) {
 int f32_create(pstep_ctx *h) {
   const Geom &G = h->geom;
   for (int d = 0; d < 3; ++d) {
-    if (G.n[d] > kMaxN || G.n[d] % kBr != 0) {
-      snprintf(h->err, sizeof h->err, "FP32 form needs cells per side a multiple of %d and at most %d", kBr, kMaxN);
+    if (G.n[d] > kMaxN || G.n[d] % kBr != 0 || G.n[d] < 2 * kBr) {
+      snprintf(h->err, sizeof h->err, "FP32 form needs cells per side a multiple of %d in [%d, %d]", kBr, 2 * kBr,
+               kMaxN);
       return PSTEP_ERR_CONFIG;
     }
   }
@@ -627,7 +830,26 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->cell_start, ncell + 1));
   TRY32(dalloc32(h, f->sidx, cap));
   TRY32(dalloc32(h, f->tmpf, cap));
+  {  // deposit work list
+    Work &w = f->work;
+    const int64_t nbk = (int64_t)(G.n[0] / kBr) * (G.n[1] / kBr) * (G.n[2] / kBr);
+    w.slot_cap = (int64_t)h->cap / kSplitMin + 1;
+    TRY32(dalloc32(h, w.items, (size_t)(nbk + 2 * w.slot_cap * 2 + 64)));
+    TRY32(dalloc32(h, w.nchunk, (size_t)nbk));
+    TRY32(dalloc32(h, w.slot, (size_t)nbk));
+    int32_t **scan_arrays[6] = {&w.cnt_a, &w.cnt_b, &w.cnt_s, &w.off_a, &w.off_b, &w.off_s};
+    for (int q = 0; q < 6; ++q) TRY32(dalloc32(h, *scan_arrays[q], (size_t)nbk + 1));
+    TRY32(dalloc32(h, w.n_items, 1));
+    TRY32(dalloc32(h, w.next, 64));
+    TRY32(dalloc32(h, w.done, (size_t)w.slot_cap));
+    TRY32(dalloc32(h, w.tiles, (size_t)w.slot_cap * 5 * kBr * kBr * kBr));
+    PSTEP_CUDA(cudaMemsetAsync(w.done, 0, sizeof(int32_t) * w.slot_cap, h->stream));
+    PSTEP_CUDA(cudaMemsetAsync(w.tiles, 0, sizeof(long long) * w.slot_cap * 5 * kBr * kBr * kBr, h->stream));
+    PSTEP_CUDA(cudaMemsetAsync(w.n_items, 0, sizeof(int32_t), h->stream));
+  }
   TRY32(dalloc32(h, f->bounds, 8));
+  TRY32(dalloc32(h, f->slots, kBoundSlots * 4));
+  PSTEP_CUDA(cudaMemsetAsync(f->slots, 0, kBoundSlots * 4 * sizeof(uint32_t), h->stream));
   TRY32(dalloc32(h, f->se, 8));
   TRY32(dalloc32(h, h->s.flag, cap));
   PSTEP_CUDA(cudaMemsetAsync(f->bounds, 0, 8 * sizeof(uint32_t), h->stream));
@@ -645,7 +867,13 @@ int f32_destroy(pstep_ctx *h) {
   dfree32(f->rhs_t); dfree32(f->itp);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx); dfree32(f->tmpf);
-  dfree32(f->bounds); dfree32(f->se);
+  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots);
+  {
+    Work &w = f->work;
+    dfree32(w.items); dfree32(w.nchunk); dfree32(w.slot); dfree32(w.cnt_a); dfree32(w.cnt_b); dfree32(w.cnt_s);
+    dfree32(w.off_a); dfree32(w.off_b); dfree32(w.off_s); dfree32(w.n_items); dfree32(w.next); dfree32(w.done);
+    dfree32(w.tiles);
+  }
   delete f;
   h->f32 = nullptr;
   return PSTEP_OK;
@@ -737,27 +965,18 @@ int f32_prime(pstep_ctx *h) {
   F32Form &f = *h->f32;
   TRY32(sort_step(h));
   const C32 c = make_c32(h, 0, 0.5, 1. / 6.);
-  PSTEP_CUDA(cudaMemsetAsync(f.bounds, 0, 4 * sizeof(uint32_t), h->stream));
   if (h->np > 0) {
     k_prime32<<<nb(h->np), kThreads, 0, h->stream>>>(h->geom, f, c.itth, h->np);
     PSTEP_LAUNCHED(h);
   }
-  // part2gas_Temp_int at the base positions: the *_new set holds them for the deposit
-  const int64_t n = h->np;
-  if (n > 0) {
-    Set32 &B = f.set[SBASE], &N = f.set[SNEW];
-    PSTEP_CUDA(cudaMemcpyAsync(N.cell, B.cell, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, h->stream));
-    for (int d = 0; d < 3; ++d)
-      PSTEP_CUDA(cudaMemcpyAsync(N.o[d], B.o[d], sizeof(float) * n, cudaMemcpyDeviceToDevice, h->stream));
-  }
-  return dep_all(h, 1);
+  // part2gas_Temp_int at the base positions
+  return dep_launch(h, false, true, f.set[SBASE], f.set[SBASE]);
 }
 
 int f32_stage(pstep_ctx *h, int k, double pre, double post) {
   F32Form &f = *h->f32;
   const C32 c = make_c32(h, k, pre, post);
   const int64_t n = h->np;
-  PSTEP_CUDA(cudaMemsetAsync(f.bounds, 0, 4 * sizeof(uint32_t), h->stream));
   prof_begin(h, PSTEP_PHASE_ADVANCE);
   if (n > 0) {
     switch (k) {
@@ -769,38 +988,42 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
     PSTEP_LAUNCHED(h);
   }
   prof_end(h, PSTEP_PHASE_ADVANCE);
+  // one walk: concentration + momentum at *_int (the base itself at stage 0), RHS_T at *_new
   prof_begin(h, PSTEP_PHASE_DEPOSIT_INT);
-  TRY32(dep_all(h, 0));
+  TRY32(dep_launch(h, true, true, f.set[h->int_is_base ? SBASE : SINT], f.set[SNEW]));
   prof_end(h, PSTEP_PHASE_DEPOSIT_INT);
-  prof_begin(h, PSTEP_PHASE_DEPOSIT_TEMP);
-  TRY32(dep_all(h, 1));
-  prof_end(h, PSTEP_PHASE_DEPOSIT_TEMP);
   return PSTEP_OK;
 }
 
 namespace {
-int dep_all(pstep_ctx *h, int mode) {
+int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   F32Form &f = *h->f32;
   const Geom &G = h->geom;
-  k_scales<<<1, 32, 0, h->stream>>>(f);
+  k_scales<<<1, 32, 0, h->stream>>>(f);  // fold this advance's maxima into the fixed-point scales
   PSTEP_LAUNCHED(h);
-  const int nbr = (G.n[0] / kBr) * (G.n[1] / kBr) * (G.n[2] / kBr);
-  if (mode == 0) {
-    // positions of the stage's *_int set (the base itself at stage 0: the FP32 form never shifts it)
-    const Set32 S = f.set[h->int_is_base ? SBASE : SINT];
-    k_dep32<0><<<nbr, kDepThreads, 0, h->stream>>>(G, f, S, h->cfg.twc, h->dep[PSTEP_FIELD_C], h->dep[PSTEP_FIELD_RU_X],
-                                                   h->dep[PSTEP_FIELD_RU_Y], h->dep[PSTEP_FIELD_RU_Z]);
-    PSTEP_LAUNCHED(h);
-    double *all[4] = {h->dep[PSTEP_FIELD_C], h->dep[PSTEP_FIELD_RU_X], h->dep[PSTEP_FIELD_RU_Y], h->dep[PSTEP_FIELD_RU_Z]};
-    // interior values are final (periodic targets): refresh the ghost layers only
-    return fold_fields(h, all, 4, 2);
+  const int grid = h->num_sms * 8;  // persistent CTAs pulling work items
+  PSTEP_CUDA(cudaMemsetAsync(f.work.next, 0, sizeof(int32_t), h->stream));
+  double *C = h->dep[PSTEP_FIELD_C], *X = h->dep[PSTEP_FIELD_RU_X], *Y = h->dep[PSTEP_FIELD_RU_Y],
+         *Z = h->dep[PSTEP_FIELD_RU_Z], *E = h->dep[PSTEP_FIELD_PART_TEMP];
+  if (do_int && do_new) {
+    k_dep32<true, true><<<grid, kDepThreads, 0, h->stream>>>(G, f, SI, SN, f.work, h->cfg.twc, C, X, Y, Z, E);
+  } else if (do_int) {
+    k_dep32<true, false><<<grid, kDepThreads, 0, h->stream>>>(G, f, SI, SN, f.work, h->cfg.twc, C, X, Y, Z, E);
+  } else {
+    k_dep32<false, true><<<grid, kDepThreads, 0, h->stream>>>(G, f, SI, SN, f.work, h->cfg.twc, C, X, Y, Z, E);
   }
-  k_dep32<1><<<nbr, kDepThreads, 0, h->stream>>>(G, f, f.set[SNEW], h->cfg.twc, h->dep[PSTEP_FIELD_PART_TEMP], nullptr, nullptr,
-                                                 nullptr);
   PSTEP_LAUNCHED(h);
-  double *e[1] = {h->dep[PSTEP_FIELD_PART_TEMP]};
-  TRY32(fold_fields(h, e, 1, 2));
-  return interior_mean(h, h->dep[PSTEP_FIELD_PART_TEMP], h->emean_dev);
+  // interior values are final (periodic targets): refresh the ghost layers only
+  if (do_int) {
+    double *all[4] = {C, X, Y, Z};
+    TRY32(fold_fields(h, all, 4, 2));
+  }
+  if (do_new) {
+    double *e[1] = {E};
+    TRY32(fold_fields(h, e, 1, 2));
+    return interior_mean(h, E, h->emean_dev);
+  }
+  return PSTEP_OK;
 }
 }  // namespace
 

@@ -4,8 +4,9 @@ Bound (uncorrected FP32 step vs the FP64 oracle): relative error <= 1e-5,
 measured norm-wise per quantity as max|fp32 - fp64| / max|fp64| (positions as
 max|dx| / L), after every step. The concentration's ghost layer is excluded:
 the reference leaves unfolded partial sums there (no refresh), the FP32 form
-periodic copies. Deposits are exact 64-bit fixed-point sums, so two runs are
-bit-identical.
+periodic copies. Deposits are exact 64-bit fixed-point sums, so two runs give
+bit-identical fields and per-particle states (compared by particle id; the
+storage order inside a cell is not fixed in this form).
 """
 import numpy as np
 import pytest
@@ -90,7 +91,9 @@ def test_fp32_deterministic(built_cuda):
         g.bind_temperature(tf)
         g.prime()
         g.run(2)
-        outs.append([g.field(helpers.FIELD_MAP[f]).copy() for f in FIELDS] + [g.array("x"), g.array("flag")])
+        order = np.argsort(g.array("flag"))
+        outs.append([g.field(helpers.FIELD_MAP[f]).copy() for f in FIELDS] +
+                    [g.array(k)[order] for k in ("x", "y", "z", "u", "v", "w", "T", "RHS_T")])
         g.close()
     for a, b in zip(*outs):
         assert helpers.bits_equal(a, b)
@@ -101,3 +104,39 @@ def test_fp32_rejects_unsupported_grid(built_cuda):
     with pytest.raises(pstep.PstepError) as e:
         pstep.ParticleStep(bp.step_config(), 100, pstep.FP32, 0)
     assert e.value.status == 2
+
+
+def test_fp32_dense_blob_split_bricks(built_cuda):
+    """A single tight blob puts tens of thousands of particles into one brick, so the
+    deposit splits it into slices combined in global memory; still within the
+    bound and bit-identical across runs."""
+    n, count = 32, 60000
+    bp = helpers.make_bp(n, count)
+    L = bp.l
+    ux, uy, uz = gen.velocity(n, 41)
+    tf = gen.temperature(n, 42)
+    x, y, z = gen.positions(n, L, 43, count, True, nblobs=1, sigma_cells=1.5)
+    u, v, w = gen.interp_velocity(n, L, x, y, z, ux, uy, uz)
+    t = np.ones(count)
+    flag = np.arange(count, dtype=np.int32)
+    arrs = [np.ascontiguousarray(a) for a in (x, y, z, u, v, w, t, flag)]
+    fields = [gen.ghost(a) for a in (ux, uy, uz, tf)]
+    o = pyoracle.Oracle(bp.step_config(), count)
+    o.load(*arrs)
+    o.prime(fields[3])
+    o.run(2, *fields)
+    outs = []
+    for _ in range(2):
+        g = pstep.ParticleStep(bp.step_config(), count, pstep.FP32, 0)
+        g.load(*arrs)
+        g.bind_velocity(*fields[:3])
+        g.bind_temperature(fields[3])
+        g.prime()
+        g.run(2)
+        e = compare(o, g, L)
+        bad = {k: v for k, v in e.items() if not v <= REL_TOL}
+        assert not bad, bad
+        outs.append([g.field(helpers.FIELD_MAP[f]).copy() for f in FIELDS])
+        g.close()
+    for a, b in zip(*outs):
+        assert helpers.bits_equal(a, b)
