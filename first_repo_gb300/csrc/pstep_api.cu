@@ -299,6 +299,21 @@ int pstep_destroy(pstep_handle h) {
   return PSTEP_OK;
 }
 
+int pstep_update_params(pstep_handle h, const pstep_config *c) {
+  if (!h || !c) return PSTEP_ERR_ARG;
+  if (c->nx != h->cfg.nx || c->ny != h->cfg.ny || c->nz != h->cfg.nz || c->bs != h->cfg.bs ||
+      c->precision != h->cfg.precision || c->capacity != h->cfg.capacity || c->lx != h->cfg.lx ||
+      c->ly != h->cfg.ly || c->lz != h->cfg.lz)
+    return fail(h, PSTEP_ERR_CONFIG, "sizes, box, precision and capacity cannot change");
+  if (!(c->dt > 0)) return fail(h, PSTEP_ERR_CONFIG, "dt must be positive");
+  h->cfg.dt = c->dt; h->cfg.tp = c->tp; h->cfg.mp = c->mp; h->cfg.dp = c->dp; h->cfg.nu = c->nu;
+  h->cfg.k = c->k; h->cfg.epsilonp = c->epsilonp; h->cfg.i0 = c->i0; h->cfg.cvp = c->cvp;
+  h->cfg.gx = c->gx; h->cfg.gy = c->gy; h->cfg.gz = c->gz;
+  h->cfg.particle_gravity = c->particle_gravity ? 1 : 0;
+  h->cfg.twc = c->twc ? 1 : 0;
+  return PSTEP_OK;
+}
+
 int pstep_set_stream(pstep_handle h, void *stream) {
   if (!h) return PSTEP_ERR_ARG;
   h->stream = (cudaStream_t)stream;

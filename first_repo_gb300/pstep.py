@@ -51,7 +51,7 @@ _D = C.POINTER(C.c_double)
 _VP = C.c_void_p
 _H = C.c_void_p
 
-EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_upload_particles", "pstep_set_tau_p",
+EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p",
            "pstep_num_particles", "pstep_bind_velocity", "pstep_bind_temperature", "pstep_prime",
            "pstep_stage_interp_advance_deposit", "pstep_wrap", "pstep_stage_temp", "pstep_stage",
            "pstep_end_stage", "pstep_end_step", "pstep_run", "pstep_get_field", "pstep_energy_mean",
@@ -67,6 +67,7 @@ def lib():
     L.pstep_create.argtypes = [C.POINTER(Config), C.POINTER(_H)]
     L.pstep_destroy.argtypes = [_H]
     L.pstep_set_stream.argtypes = [_H, _VP]
+    L.pstep_update_params.argtypes = [_H, C.POINTER(Config)]
     L.pstep_upload_particles.argtypes = [_H, C.c_int64] + [_VP] * 8 + [C.c_int]
     L.pstep_set_tau_p.argtypes = [_H, _VP, C.c_int]
     L.pstep_num_particles.argtypes = [_H]

@@ -113,6 +113,10 @@ int pstep_create(const pstep_config *cfg, pstep_handle *out);
 int pstep_destroy(pstep_handle h);
 /* Stream for all work of this handle (cudaStream_t; 0 = legacy default). */
 int pstep_set_stream(pstep_handle h, void *cuda_stream);
+/* Update the scalar parameters (dt, tp, mp, dp, nu, k, epsilonp, i0, cvp, gravity,
+ * twc) that params::update switches after its threshold (params.cpp:66-77).
+ * Sizes, precision, flags and capacity must not change. */
+int pstep_update_params(pstep_handle h, const pstep_config *cfg);
 
 /* Set the base particle state x,u,T and flag for n particles (the reference's
  * load_random / Load_All leave these in the public vectors, particle.cpp:919-999).

@@ -60,3 +60,31 @@ def test_null_handle_is_an_error(built_cuda):
     assert L.pstep_prime(None) == 1
     assert L.pstep_end_step(None) == 1
     assert L.pstep_num_particles(None) == -1
+
+
+REFDIR = "/root/reference"
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REFDIR, "particle.h")), reason="reference headers not present")
+def test_adapter_compiles_and_links_against_reference_headers(built_cuda, tmp_path):
+    """first_repo_gb300/adapter/particle_gpu.cpp builds in place of the reference's
+    particle.cpp against its unchanged particle.h, and links with the reference's
+    other sources and libpstep.so (running it needs a GPU)."""
+    obj = tmp_path / "particle_gpu.o"
+    cmd = ["g++", "-std=c++11", "-O1", "-w", "-I", os.path.join(ROOT, "oracle", "mpi_stub"), "-I", REFDIR,
+           "-I", os.path.join(ROOT, "include"), "-c", os.path.join(ROOT, "first_repo_gb300", "adapter", "particle_gpu.cpp"),
+           "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    main = tmp_path / "main.cpp"
+    main.write_text('#include "mpi.h"\n#include "params.h"\n#include "proc.h"\n#include "gridsize.h"\n'
+                    '#include "particle.h"\nint main(int c, char **v) { if (c < 2) return 0; MPI_Init(&c, &v);\n'
+                    'params p(v[1]); proc pc; gridsize s(&p, &pc); particle part(&p, &pc, &s); return 0; }\n')
+    srcs = [os.path.join(REFDIR, f) for f in ("tensor0.cpp", "tensor1.cpp", "communicator.cpp", "gridsize.cpp",
+                                              "proc.cpp", "params.cpp")]
+    exe = tmp_path / "app"
+    cmd = ["g++", "-std=c++11", "-O1", "-w", "-I", os.path.join(ROOT, "oracle", "mpi_stub"), "-I", REFDIR,
+           str(main), str(obj), *srcs, "-L", os.path.dirname(_lib.path("libpstep.so")), "-lpstep",
+           "-L/usr/local/cuda/lib64", "-lcudart", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
