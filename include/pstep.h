@@ -174,6 +174,21 @@ int pstep_energy_mean(pstep_handle h, double *out);
  * in the reference's order when PSTEP_TRACK_ORDER is set. */
 int pstep_get_particle_array(pstep_handle h, int array_id, void *dst, int on_device);
 
+/* Interior mean of a ghosted field ((nx+2)(ny+2)(nz+2) doubles, device pointer),
+ * written to *out (device pointer), enqueued on `stream`; the same quantity as
+ * pstep_energy_mean. No counterpart in the reference (whose tensor0::mean runs on
+ * the host): this entry point allocates no device memory, for callers that cannot
+ * call cudaMalloc (work recorded during CUDA stream capture, applications whose own
+ * pool owns device memory, loops that must not synchronise the device). Its
+ * scratch is a fixed device array of 2^20 row sums (8 MiB, held by every GPU that
+ * loads the library until the process exits): ny*nz above 2^20 returns
+ * PSTEP_ERR_CAPACITY. The first call on a device looks up that array's address
+ * (make it before any stream capture). Every call writes all the scratch it reads,
+ * so nothing needs clearing, but all calls share the array: calls that overlap on
+ * the GPU race. Messages: pstep_noalloc_last_error(). */
+int pstep_field_mean_noalloc(const double *field, int32_t nx, int32_t ny, int32_t nz, double *out, void *stream);
+const char *pstep_noalloc_last_error(void);
+
 /* Error reporting */
 const char *pstep_last_error(pstep_handle h);
 const char *pstep_status_string(int status);
