@@ -8,15 +8,15 @@ import subprocess
 import pytest
 
 import helpers  # noqa: F401  (sets sys.path)
-from first_repo_gb300 import _lib, pstep
+from first_repo_gb300 import _lib, mlp, pstep
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared(header):
+def declared(header, prefix="pstep_"):
     src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(pstep_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(" + prefix + r"[a-z0-9_]+)\s*\(", src)))
 
 
 def test_header_declares_the_binding_surface():
@@ -31,6 +31,17 @@ def test_library_exports_every_declared_symbol(built_cuda):
     out = subprocess.run(["nm", "-D", "--defined-only", _lib.path("libpstep.so")], capture_output=True, text=True).stdout
     exported = set(re.findall(r"\b(pstep_[a-z0-9_]+)\b", out))
     for name in declared("pstep.h"):
+        assert name in exported, name
+
+
+def test_mlp_header_matches_binding_and_exports(built_cuda):
+    names = declared("pstep_mlp.h", "pmlp_")
+    assert set(mlp.EXPORTS) == set(names)
+    lib = ctypes.CDLL(_lib.path("libpstep.so"))
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.path("libpstep.so")], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\b(pmlp_[a-z0-9_]+)\b", out))
+    for name in names:
+        assert hasattr(lib, name), name
         assert name in exported, name
 
 
