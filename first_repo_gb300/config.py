@@ -40,6 +40,12 @@ class BoxParams:
     gz: float = 0.0
     twc: int = 1
     particle_gravity: int = 0
+    # gas-step settings (params.in lines Cooling, iterations/convergence, A1 A2, U0)
+    cooling: int = 0
+    iterations: int = 30
+    epsilon: float = 1e-7
+    a_force: float = 0.0
+    u0: float = 0.0
 
     def derived(self) -> dict:
         """params.cpp:51-56 in the reference's operand order."""
@@ -59,13 +65,23 @@ class BoxParams:
                     epsilonp=self.epsilonp, i0=self.i0, cvp=self.cvp, gx=self.gx, gy=self.gy, gz=self.gz,
                     particle_gravity=self.particle_gravity, twc=self.twc)
 
+    def gas_config(self) -> dict:
+        """The scalars the box gas step consumes (grid.cpp; params.cpp:22-56)."""
+        d = self.derived()
+        return dict(n=self.n, l=self.l, dt=self.dt, mu0=self.mu0, k=self.k, cp=self.cp, cv=self.cv, rho0=self.rho0,
+                    u0=self.u0, a_force=self.a_force, gx=self.gx, gy=self.gy, gz=self.gz, mp=d["mp"],
+                    epsilon=self.epsilon, iterations=self.iterations, cooling=self.cooling, twc=self.twc,
+                    p0=d["P0"])
+
     def params_file(self) -> str:
         """A parameter file in the reference's positional format (params.cpp:22-48)."""
         r = repr
         lines = [
             "1", f"{self.n} {self.n} {self.n}", f"{r(self.l)} {r(self.l)} {r(self.l)}", "1", "0",
-            f"1 {r(self.dt)} 1e30", "0 0", "1000000 1000000", "./ ./", "2", "0 0", "0", "30 30 1e-7",
-            f"{self.twc} {self.particle_gravity}", "0 0", r(self.rho0), "0", r(self.t0),
+            f"1 {r(self.dt)} 1e30", "0 0", "1000000 1000000", "./ ./", "2", "0 0", str(self.cooling),
+            f"{self.iterations} {self.iterations} {r(self.epsilon)}",
+            f"{self.twc} {self.particle_gravity}", f"{r(self.a_force)} {r(self.a_force)}", r(self.rho0),
+            r(self.u0), r(self.t0),
             f"{r(self.mu0)} {r(self.k)}",
             f"{r(self.gx)} {r(self.gy)} {r(self.gz)} {r(self.gx)} {r(self.gy)} {r(self.gz)}",
             f"{r(self.cp)} {r(self.cv)}", r(self.np0), f"{r(self.dp)} {r(self.rhop)}", r(self.cvp),

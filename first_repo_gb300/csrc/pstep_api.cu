@@ -56,6 +56,7 @@ int f32_destroy(pstep_ctx *h);
 int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, const double *u, const double *v,
                const double *w, const double *t, int on_device);
 int f32_set_tau(pstep_ctx *h, const double *tau, int on_device);
+int f32_set_props(pstep_ctx *h, const pstep_particle_props *props, int on_device);
 int f32_bind_fields(pstep_ctx *h);
 int f32_prime(pstep_ctx *h);
 int f32_stage(pstep_ctx *h, int k, double pre, double post);
@@ -390,6 +391,15 @@ int pstep_set_tau_p(pstep_handle h, const double *tau, int on_device) {
   return PSTEP_OK;
 }
 
+int pstep_set_particle_props(pstep_handle h, const pstep_particle_props *props, int on_device) {
+  if (!h || !props) return PSTEP_ERR_ARG;
+  if (is_f32(h)) return f32_set_props(h, props, on_device);
+  if (props->mass_ratio || props->itth || props->heat_is || props->alpha || props->accel[0] || props->accel[1] ||
+      props->accel[2])
+    return fail(h, PSTEP_ERR_CONFIG, "per-particle properties other than tau_p need the FP32 form");
+  return pstep_set_tau_p(h, props->tau_p, on_device);
+}
+
 int pstep_bind_velocity(pstep_handle h, const double *ux, const double *uy, const double *uz, int on_device) {
   if (!h) return PSTEP_ERR_ARG;
   TRY(copy_field_in(h, ux, on_device, h->own_u[0], h->ux));
@@ -610,6 +620,7 @@ int pstep_get_particle_array(pstep_handle h, int id, void *dst, int on_device) {
   const int64_t n = h->np;
   if (n == 0) return PSTEP_OK;
   if (is_f32(h) && id != PSTEP_FLAG) return f32_get_array(h, id, dst, on_device);
+  if (id >= PSTEP_UG) return fail(h, PSTEP_ERR_CONFIG, "gas values per particle are kept by the FP32 form");
   const int32_t *perm = (h->cfg.flags & PSTEP_TRACK_ORDER) ? h->phys_of_ref : nullptr;
   if (id == PSTEP_FLAG) {
     int32_t *tmp = (int32_t *)h->perm_tmp;

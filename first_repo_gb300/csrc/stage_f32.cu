@@ -79,6 +79,8 @@ struct F32Form {
   Set32 set[4];
   float *rhs_t;
   float *itp;      // per-particle 1/tau_p or nullptr
+  float *pp[7];    // per-particle mass ratio, itth, 1/(m Cvp), alpha, body acceleration x y z (or nullptr)
+  float *gas[4];   // ug vg wg at x_int and Tg - t_ref at x_new of the last stage (PSTEP_KEEP_GAS)
   float *rhs_u[3];
   float *uf[3], *tf;  // fp32 ghosted copies of the bound fields
   uint32_t *key;      // brick-major cell id of the base position
@@ -157,6 +159,8 @@ struct C32 {
   float itp, g[3], alpha, itth;
 };
 
+enum { PP_MASS = 0, PP_ITTH, PP_HEAT_IS, PP_ALPHA, PP_ACC };  // F32Form::pp slots (PP_ACC + d)
+
 template <int K>
 __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int twc, int64_t n,
                                                    int32_t *__restrict__ err) {
@@ -176,6 +180,13 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
     for (int q = 0; q < 4; ++q) { vb[q] = B.v[q][p]; vin[q] = I.v[q][p]; vac[q] = A.v[q][p]; }
     const float rhs_t_old = f.rhs_t[p];
     const float itp = f.itp ? f.itp[p] : c.itp;
+    const float itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
+    const float alpha = f.pp[PP_ALPHA] ? f.pp[PP_ALPHA][p] : c.alpha;
+    const float dpre_is = f.pp[PP_HEAT_IS] ? c.dt_pre * f.pp[PP_HEAT_IS][p] : c.dt_pre_is;
+    const float dpost_is = f.pp[PP_HEAT_IS] ? c.dt_post * f.pp[PP_HEAT_IS][p] : c.dt_post_is;
+    float gacc[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) gacc[d] = f.pp[PP_ACC + d] ? f.pp[PP_ACC + d][p] : c.g[d];
 
     // face-normal interpolation at x_int (particle.cpp:340-360)
     const int ii = ci_(cint) + 1, jj = cj_(cint) + 1, kk = ck_(cint) + 1;
@@ -208,11 +219,11 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       rhs[d] = (gas[d] - vin[d]) * itp;
-      vac[d] += c.dt_post * (rhs[d] + c.g[d]);
-      vn[d] = (K != 3) ? vb[d] + c.dt_pre * (rhs[d] + c.g[d]) : vac[d];
+      vac[d] += c.dt_post * (rhs[d] + gacc[d]);
+      vn[d] = (K != 3) ? vb[d] + c.dt_pre * (rhs[d] + gacc[d]) : vac[d];
     }
-    vac[3] += c.dt_post_is * (rhs_t_old + c.alpha);
-    vn[3] = (K != 3) ? vb[3] + c.dt_pre_is * (rhs_t_old + c.alpha) : vac[3];
+    vac[3] += dpost_is * (rhs_t_old + alpha);
+    vn[3] = (K != 3) ? vb[3] + dpre_is * (rhs_t_old + alpha) : vac[3];
 
     // trilinear T at x_new (particle.cpp:430-456): node = cell + h, x_l = o - h + 1/2
     const int hx = on[0] >= 0.5f, hy = on[1] >= 0.5f, hz = on[2] >= 0.5f;
@@ -225,7 +236,7 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
                      (1.f - tx) * ty * (1.f - tz) * T[glin3(G, ni - 1, nj, nk - 1)] +
                      tx * (1.f - ty) * (1.f - tz) * T[glin3(G, ni, nj - 1, nk - 1)] +
                      (1.f - tx) * (1.f - ty) * (1.f - tz) * T[glin3(G, ni - 1, nj - 1, nk - 1)];
-    const float rhs_t_new = (tg - vn[3]) * c.itth;
+    const float rhs_t_new = (tg - vn[3]) * itth;
     if (!isfinite(rhs_t_new) || !isfinite(vn[0]) || !isfinite(vn[1]) || !isfinite(vn[2]) || !isfinite(on[0]) ||
         !isfinite(on[1]) || !isfinite(on[2]))
       atomicOr(err, kErrNonFinite);
@@ -239,12 +250,19 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
     for (int d = 0; d < 3; ++d) { N.o[d][p] = on[d]; P.o[d][p] = oac[d]; }
 #pragma unroll
     for (int q = 0; q < 4; ++q) { N.v[q][p] = vn[q]; P.v[q][p] = vac[q]; }
+    // the momentum deposit carries the particle's mass relative to cfg.mp
+    const float mrel = f.pp[PP_MASS] ? f.pp[PP_MASS][p] : 1.f;
     if (twc) {
 #pragma unroll
-      for (int d = 0; d < 3; ++d) f.rhs_u[d][p] = rhs[d];
+      for (int d = 0; d < 3; ++d) f.rhs_u[d][p] = rhs[d] * mrel;
     }
     f.rhs_t[p] = rhs_t_new;
-    mu0 = rhs[0]; mu1 = rhs[1]; mu2 = rhs[2]; mt = rhs_t_new;
+    if (f.gas[0]) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) f.gas[d][p] = gas[d];
+      f.gas[3][p] = tg;
+    }
+    mu0 = rhs[0] * mrel; mu1 = rhs[1] * mrel; mu2 = rhs[2] * mrel; mt = rhs_t_new;
   }
   // bounds for the fixed-point scales (order-independent maxima)
   block_max4(f.slots, fabsf(mu0), fabsf(mu1), fabsf(mu2), fabsf(mt));
@@ -268,7 +286,7 @@ __global__ void k_prime32(Geom G, F32Form f, float itth, int64_t n) {
                      (1.f - tx) * ty * (1.f - tz) * T[glin3(G, ni - 1, nj, nk - 1)] +
                      tx * (1.f - ty) * (1.f - tz) * T[glin3(G, ni, nj - 1, nk - 1)] +
                      (1.f - tx) * (1.f - ty) * (1.f - tz) * T[glin3(G, ni - 1, nj - 1, nk - 1)];
-    mt = (tg - B.v[3][p]) * itth;
+    mt = (tg - B.v[3][p]) * (f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : itth);
     f.rhs_t[p] = mt;
   }
   block_max4(f.slots, 0.f, 0.f, 0.f, fabsf(mt));
@@ -692,6 +710,11 @@ __global__ void k_f32_to_f64(const float *__restrict__ src, int64_t n, double *_
   if (i < n) dst[i] = (double)src[i];
 }
 
+__global__ void k_to_f32_shift(const float *__restrict__ src, int64_t n, double shift, double *__restrict__ dst) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (double)src[i] + shift;
+}
+
 __global__ void k_recip32(const double *__restrict__ tau, int64_t n, float *__restrict__ out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = (float)(1. / tau[i]);
@@ -771,6 +794,10 @@ int sort_step(pstep_ctx *h) {
     for (int q = 0; q < 4; ++q) permf(B.v[q]);
     permf(f.rhs_t);
     if (f.itp) permf(f.itp);
+    for (int q = 0; q < 7; ++q)
+      if (f.pp[q]) permf(f.pp[q]);
+    for (int q = 0; q < 4; ++q)
+      if (f.gas[q]) permf(f.gas[q]);
     {
       k_perm<uint32_t><<<nb(n), kThreads, 0, h->stream>>>(B.cell, f.sidx, n, (uint32_t *)f.tmpf);
       uint32_t *t = B.cell; B.cell = (uint32_t *)f.tmpf; f.tmpf = (float *)t;
@@ -822,6 +849,11 @@ int f32_create(pstep_ctx *h) {
   }
   TRY32(dalloc32(h, f->rhs_t, cap));
   for (int d = 0; d < 3; ++d) TRY32(dalloc32(h, f->rhs_u[d], cap));
+  if (h->cfg.flags & PSTEP_KEEP_GAS)
+    for (int q = 0; q < 4; ++q) {
+      TRY32(dalloc32(h, f->gas[q], cap));
+      PSTEP_CUDA(cudaMemsetAsync(f->gas[q], 0, sizeof(float) * cap, h->stream));
+    }
   const size_t gs = (size_t)G.gsize;
   for (int d = 0; d < 3; ++d) TRY32(dalloc32(h, f->uf[d], gs));
   TRY32(dalloc32(h, f->tf, gs));
@@ -865,6 +897,8 @@ int f32_destroy(pstep_ctx *h) {
     for (int q = 0; q < 4; ++q) dfree32(f->set[s].v[q]);
   }
   dfree32(f->rhs_t); dfree32(f->itp);
+  for (int q = 0; q < 7; ++q) dfree32(f->pp[q]);
+  for (int q = 0; q < 4; ++q) dfree32(f->gas[q]);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx); dfree32(f->tmpf);
   dfree32(f->bounds); dfree32(f->se); dfree32(f->slots);
@@ -884,6 +918,7 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
   F32Form &f = *h->f32;
   const int64_t n = h->np;
   dfree32(f.itp);
+  for (int q = 0; q < 7; ++q) dfree32(f.pp[q]);
   f.sorted = 0;
   if (n == 0) return PSTEP_OK;
   if (!f.tref_set) {
@@ -934,6 +969,44 @@ int f32_set_tau(pstep_ctx *h, const double *tau, int on_device) {
   }
   k_recip32<<<nb(n), kThreads, 0, h->stream>>>(src, n, f.itp);
   PSTEP_LAUNCHED(h);
+  if (tmp) {
+    PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+    dfree32(tmp);
+  }
+  return PSTEP_OK;
+}
+
+__global__ void k_d2f(const double *__restrict__ src, int64_t n, float *__restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)src[i];
+}
+
+int f32_set_props(pstep_ctx *h, const pstep_particle_props *pr, int on_device) {
+  F32Form &f = *h->f32;
+  if (f.sorted) {
+    snprintf(h->err, sizeof h->err, "particle properties must be set before pstep_prime");
+    return PSTEP_ERR_STATE;
+  }
+  TRY32(f32_set_tau(h, pr->tau_p, on_device));
+  const double *src[7] = {pr->mass_ratio, pr->itth, pr->heat_is, pr->alpha, pr->accel[0], pr->accel[1], pr->accel[2]};
+  const int64_t n = h->np;
+  double *tmp = nullptr;
+  if (!on_device && n > 0) TRY32(dalloc32(h, tmp, (size_t)n));
+  for (int q = 0; q < 7; ++q) {
+    if (!src[q]) {
+      dfree32(f.pp[q]);
+      continue;
+    }
+    if (!f.pp[q]) TRY32(dalloc32(h, f.pp[q], (size_t)h->cap));
+    if (n == 0) continue;
+    const double *s = src[q];
+    if (!on_device) {
+      PSTEP_CUDA(cudaMemcpyAsync(tmp, src[q], sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+      s = tmp;
+    }
+    k_d2f<<<nb(n), kThreads, 0, h->stream>>>(s, n, f.pp[q]);
+    PSTEP_LAUNCHED(h);
+  }
   if (tmp) {
     PSTEP_CUDA(cudaStreamSynchronize(h->stream));
     dfree32(tmp);
@@ -1055,10 +1128,16 @@ int f32_get_array(pstep_ctx *h, int id, void *dst, int on_device) {
   else if (id <= PSTEP_T_NEW) { set = h->phase != 0 ? SNEW : (h->int_is_base ? SBASE : SINT); comp = id - PSTEP_X_NEW; }
   else if (id <= PSTEP_T_NP1) { set = h->np1_is_base ? SBASE : SNP1; comp = id - PSTEP_X_NP1; }
   else set = -1;
+  if (id >= PSTEP_UG && !f.gas[0]) {
+    snprintf(h->err, sizeof h->err, "gas values per particle need the PSTEP_KEEP_GAS flag");
+    return PSTEP_ERR_CONFIG;
+  }
   double *tmp = nullptr;
   TRY32(dalloc32(h, tmp, (size_t)n));
   if (set >= 0) {
     k_to_f64_arr<<<nb(n), kThreads, 0, h->stream>>>(h->geom, f.set[set], comp, f.tref, n, tmp);
+  } else if (id >= PSTEP_UG) {
+    k_to_f32_shift<<<nb(n), kThreads, 0, h->stream>>>(f.gas[id - PSTEP_UG], n, id == PSTEP_TG ? f.tref : 0.0, tmp);
   } else {
     k_f32_to_f64<<<nb(n), kThreads, 0, h->stream>>>(f.rhs_t, n, tmp);  // RHS_T
   }

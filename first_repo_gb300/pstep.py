@@ -16,14 +16,14 @@ from . import _lib
 from .config import RK4_POST, RK4_PRE
 
 FP64, FP32 = 0, 1
-TRACK_ORDER, CHECK_INPUTS, REFERENCE_SUMS = 1, 2, 4
+TRACK_ORDER, CHECK_INPUTS, REFERENCE_SUMS, KEEP_GAS = 1, 2, 4, 8
 
 ARRAY_IDS = {n: i for i, n in enumerate(
     ["x", "y", "z", "u", "v", "w", "T",
      "x_int", "y_int", "z_int", "u_int", "v_int", "w_int", "T_int",
      "x_new", "y_new", "z_new", "u_new", "v_new", "w_new", "T_new",
      "x_np1", "y_np1", "z_np1", "u_np1", "v_np1", "w_np1", "T_np1",
-     "RHS_T", "flag"])}
+     "RHS_T", "flag", "ug", "vg", "wg", "Tg"])}
 FIELD_IDS = {"C": 0, "RHS_RU_x": 1, "RHS_RU_y": 2, "RHS_RU_z": 3, "RHS_Part_Temp": 4}
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported configuration", 3: "capacity exceeded",
@@ -35,6 +35,11 @@ class PstepError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"pstep status {status} ({STATUS.get(status, '?')}): {msg}")
         self.status = status
+
+
+class Props(C.Structure):
+    _fields_ = [("tau_p", C.c_void_p), ("mass_ratio", C.c_void_p), ("itth", C.c_void_p), ("heat_is", C.c_void_p),
+                ("alpha", C.c_void_p), ("accel", C.c_void_p * 3)]
 
 
 class Config(C.Structure):
@@ -51,7 +56,7 @@ _D = C.POINTER(C.c_double)
 _VP = C.c_void_p
 _H = C.c_void_p
 
-EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p",
+EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p", "pstep_set_particle_props",
            "pstep_num_particles", "pstep_bind_velocity", "pstep_bind_temperature", "pstep_prime",
            "pstep_stage_interp_advance_deposit", "pstep_wrap", "pstep_stage_temp", "pstep_stage",
            "pstep_end_stage", "pstep_end_step", "pstep_run", "pstep_get_field", "pstep_energy_mean",
@@ -70,6 +75,7 @@ def lib():
     L.pstep_update_params.argtypes = [_H, C.POINTER(Config)]
     L.pstep_upload_particles.argtypes = [_H, C.c_int64] + [_VP] * 8 + [C.c_int]
     L.pstep_set_tau_p.argtypes = [_H, _VP, C.c_int]
+    L.pstep_set_particle_props.argtypes = [_H, C.POINTER(Props), C.c_int]
     L.pstep_num_particles.argtypes = [_H]
     L.pstep_num_particles.restype = C.c_int64
     L.pstep_bind_velocity.argtypes = [_H, _VP, _VP, _VP, C.c_int]
@@ -170,6 +176,36 @@ class ParticleStep:
         else:
             p, d = _ptr(tau)
             self._ok(self.L.pstep_set_tau_p(self.h, p, d))
+
+    def set_props(self, tau_p=None, mass_ratio=None, itth=None, heat_is=None, alpha=None, accel=None):
+        """Per-particle properties in upload order (pstep_set_particle_props); None keeps
+        the config's scalar. accel is a sequence of three arrays (or None)."""
+        pr = Props()
+        keep = []
+        on_dev = None
+
+        def addr(a):
+            nonlocal on_dev
+            if a is None:
+                return None
+            if isinstance(a, np.ndarray):
+                a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            p, d = _ptr(a)
+            if on_dev is not None and on_dev != d:
+                raise ValueError("mix of host and device property arrays")
+            on_dev = d
+            return p
+
+        pr.tau_p = addr(tau_p)
+        pr.mass_ratio = addr(mass_ratio)
+        pr.itth = addr(itth)
+        pr.heat_is = addr(heat_is)
+        pr.alpha = addr(alpha)
+        if accel is not None:
+            for d in range(3):
+                pr.accel[d] = addr(accel[d])
+        self._ok(self.L.pstep_set_particle_props(self.h, C.byref(pr), int(on_dev or 0)))
 
     @property
     def np(self) -> int:

@@ -62,9 +62,12 @@ enum { PSTEP_FP64 = 0, PSTEP_FP32 = 1 };
 enum {
   PSTEP_TRACK_ORDER = 1,     /* keep the reference's particle order for downloads (FP64 only) */
   PSTEP_CHECK_INPUTS = 2,    /* validate uploads (finite, in range) before use */
-  PSTEP_REFERENCE_SUMS = 4   /* with TRACK_ORDER: add every deposit in the reference's particle
+  PSTEP_REFERENCE_SUMS = 4,  /* with TRACK_ORDER: add every deposit in the reference's particle
                                 order, so deposited fields are bit-identical to the reference
                                 (slower; without it the order is fixed but different) */
+  PSTEP_KEEP_GAS = 8         /* FP32: keep the gas values each particle's update used (the
+                                reference's public ug/vg/wg/Tg, particle.h:110-113) for
+                                pstep_get_particle_array (16 bytes per particle and stage) */
 };
 
 /* Scalars of params.h that the particle step reads (params.cpp:22-56). The
@@ -93,6 +96,9 @@ enum {
   PSTEP_X_NP1, PSTEP_Y_NP1, PSTEP_Z_NP1, PSTEP_U_NP1, PSTEP_V_NP1, PSTEP_W_NP1, PSTEP_T_NP1,
   PSTEP_RHS_T,               /* particle.h:116 */
   PSTEP_FLAG,                /* int32 particle id (particle.h:119) */
+  PSTEP_UG, PSTEP_VG, PSTEP_WG, /* gas velocity at x_int used by the last stage (gas2part_velocity,
+                                   particle.cpp:340-360); FP32 with PSTEP_KEEP_GAS */
+  PSTEP_TG,                  /* gas temperature at x_new used by the last stage (particle.cpp:430-456) */
   PSTEP_NUM_ARRAYS
 };
 
@@ -128,6 +134,22 @@ int pstep_upload_particles(pstep_handle h, int64_t n, const double *x, const dou
 /* Optional per-particle momentum relaxation time (same order as the upload);
  * replaces the scalar Tp for every particle. NULL restores the scalar. */
 int pstep_set_tau_p(pstep_handle h, const double *tau_p, int on_device);
+
+/* Per-particle physical properties. No reference counterpart: the reference's
+ * particles share the scalars of params.h. Each pointer holds one value per
+ * particle in upload order, or is NULL to keep the config's scalar. Set after
+ * pstep_upload_particles and before pstep_prime; FP32 form (the FP64 form
+ * accepts tau_p alone). */
+typedef struct pstep_particle_props {
+  const double *tau_p;       /* momentum relaxation time (replaces Tp, particle.cpp:365) */
+  const double *mass_ratio;  /* m_p / cfg.mp: weight of the momentum deposit (the gas scales
+                                RHS_RU by -mp/Vcell, grid.cpp:393) */
+  const double *itth;        /* heat-transfer coefficient Nu*PI*Dp*k (particle.cpp:462) */
+  const double *heat_is;     /* 1/(m_p*Cvp) (particle.cpp:485) */
+  const double *alpha;       /* absorbed power 0.25*epsilonp*PI*Dp^2*I0 (particle.cpp:484) */
+  const double *accel[3];    /* body acceleration, replaces ParticleGravity*g (particle.cpp:376-378) */
+} pstep_particle_props;
+int pstep_set_particle_props(pstep_handle h, const pstep_particle_props *props, int on_device);
 int64_t pstep_num_particles(pstep_handle h);
 
 /* Gas fields, ghosted layout. The velocity is U = RU_int/Rho_face (grid.cpp:662),

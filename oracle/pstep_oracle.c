@@ -32,7 +32,18 @@ struct pso_state {
   double *a[PSO_NARRAYS];
   int32_t *flag;
   double *rec0, *rec1; /* leaver records: 29 doubles each (ToBuf layout) */
+  double *prop[8];      /* per-particle properties by id (pso_set_props) or NULL */
+  int64_t nprop;
 };
+
+enum { PR_TAU, PR_MASS, PR_ITTH, PR_HEAT_IS, PR_ALPHA, PR_AX, PR_AY, PR_AZ };
+
+/* property q of the particle at storage index i, or the scalar fallback */
+static double prop_or(const pso_state *s, int q, int64_t i, double scalar) {
+  if (!s->prop[q]) return scalar;
+  const int32_t id = s->flag[i];
+  return (id >= 0 && id < s->nprop) ? s->prop[q][id] : scalar;
+}
 
 #define G(s) ((s)->c.n + 2)
 #define AT(f, s, i, j, k) (f)[((size_t)(k) * G(s) + (size_t)(j)) * G(s) + (size_t)(i)]
@@ -55,6 +66,7 @@ pso_state *pso_create(const pso_config *cfg, int64_t capacity) {
 void pso_destroy(pso_state *s) {
   if (!s) return;
   for (int i = 0; i < PSO_NARRAYS; ++i) free(s->a[i]);
+  for (int q = 0; q < 8; ++q) free(s->prop[q]);
   free(s->flag); free(s->rec0); free(s->rec1);
   free(s);
 }
@@ -160,7 +172,21 @@ static void gas2part_temp(pso_state *s, int px, int py, int pz, const double *T)
 static void compute_rhs_temp(pso_state *s, int tid) {
   double iTth = s->c.nu * PSO_PI * s->c.dp * s->c.k;
   double *Tg = s->a[PSO_TG], *Tp = s->a[tid], *R = s->a[PSO_RHS_T];
-  for (int64_t i = 0; i < s->np; ++i) R[i] = (Tg[i] - Tp[i]) * iTth;
+  for (int64_t i = 0; i < s->np; ++i) R[i] = (Tg[i] - Tp[i]) * prop_or(s, PR_ITTH, i, iTth);
+}
+
+int pso_set_props(pso_state *s, int64_t n, const double *tau_p, const double *mass_ratio, const double *itth,
+                  const double *heat_is, const double *alpha, const double *ax, const double *ay, const double *az) {
+  const double *src[8] = {tau_p, mass_ratio, itth, heat_is, alpha, ax, ay, az};
+  for (int q = 0; q < 8; ++q) {
+    free(s->prop[q]);
+    s->prop[q] = 0;
+    if (!src[q] || n <= 0) continue;
+    s->prop[q] = (double *)malloc(sizeof(double) * (size_t)n);
+    memcpy(s->prop[q], src[q], sizeof(double) * (size_t)n);
+  }
+  s->nprop = n;
+  return 0;
 }
 
 /* particle.cpp:526-559 (weights w) and :586-658 (weights w * RHS_T), trilinear at round() nodes */
@@ -313,10 +339,20 @@ int pso_stage(pso_state *s, int k, const double *ux, const double *uy, const dou
     for (int d = 0; d < 3; ++d) {
       double *rhs = s->a[PSO_RHS_U + d], *vin = s->a[PSO_U_INT + d], *np1 = s->a[PSO_U_NP1 + d],
              *nw = s->a[PSO_U_NEW + d], *b = s->a[PSO_U + d];
-      for (int64_t i = 0; i < n; ++i) rhs[i] = (gas[d][i] - vin[i]) * iTp;
-      for (int64_t i = 0; i < n; ++i) np1[i] += dt * Q * (rhs[i] + g[d]);
-      if (k != 3) for (int64_t i = 0; i < n; ++i) nw[i] = b[i] + dt * P * (rhs[i] + g[d]);
-      else for (int64_t i = 0; i < n; ++i) nw[i] = np1[i];
+      if (!s->prop[PR_TAU] && !s->prop[PR_AX + d]) {
+        for (int64_t i = 0; i < n; ++i) rhs[i] = (gas[d][i] - vin[i]) * iTp;
+        for (int64_t i = 0; i < n; ++i) np1[i] += dt * Q * (rhs[i] + g[d]);
+        if (k != 3) for (int64_t i = 0; i < n; ++i) nw[i] = b[i] + dt * P * (rhs[i] + g[d]);
+        else for (int64_t i = 0; i < n; ++i) nw[i] = np1[i];
+      } else {
+        for (int64_t i = 0; i < n; ++i) {
+          const double itp_i = s->prop[PR_TAU] ? 1. / prop_or(s, PR_TAU, i, 0.0) : iTp;
+          const double g_i = prop_or(s, PR_AX + d, i, g[d]);
+          rhs[i] = (gas[d][i] - vin[i]) * itp_i;
+          np1[i] += dt * Q * (rhs[i] + g_i);
+          nw[i] = (k != 3) ? b[i] + dt * P * (rhs[i] + g_i) : np1[i];
+        }
+      }
     }
   }
   /* update_Temp :480-496 */
@@ -324,9 +360,17 @@ int pso_stage(pso_state *s, int k, const double *ux, const double *uy, const dou
     double alpha = 0.25 * s->c.epsilonp * PSO_PI * s->c.dp * s->c.dp * s->c.i0;
     double iS = 1. / (s->c.mp * s->c.cvp);
     double *np1 = s->a[PSO_T_NP1], *nw = s->a[PSO_T_NEW], *b = s->a[PSO_T], *R = s->a[PSO_RHS_T];
-    for (int64_t i = 0; i < n; ++i) np1[i] += dt * Q * iS * (R[i] + alpha);
-    if (k != 3) for (int64_t i = 0; i < n; ++i) nw[i] = b[i] + dt * P * iS * (R[i] + alpha);
-    else for (int64_t i = 0; i < n; ++i) nw[i] = np1[i];
+    if (!s->prop[PR_HEAT_IS] && !s->prop[PR_ALPHA]) {
+      for (int64_t i = 0; i < n; ++i) np1[i] += dt * Q * iS * (R[i] + alpha);
+      if (k != 3) for (int64_t i = 0; i < n; ++i) nw[i] = b[i] + dt * P * iS * (R[i] + alpha);
+      else for (int64_t i = 0; i < n; ++i) nw[i] = np1[i];
+    } else {
+      for (int64_t i = 0; i < n; ++i) {
+        const double is_i = prop_or(s, PR_HEAT_IS, i, iS), a_i = prop_or(s, PR_ALPHA, i, alpha);
+        np1[i] += dt * Q * is_i * (R[i] + a_i);
+        nw[i] = (k != 3) ? b[i] + dt * P * is_i * (R[i] + a_i) : np1[i];
+      }
+    }
   }
   /* part2gas_concentration :526-559 (no refresh) */
   part2gas_trilinear(s, PSO_X_INT, PSO_Y_INT, PSO_Z_INT, 0, c, 0);
@@ -340,12 +384,17 @@ int pso_stage(pso_state *s, int k, const double *ux, const double *uy, const dou
       double y_l = (yi[i] * idx - ((int)(yi[i] * idx)));
       double z_l = (zi[i] * idx - ((int)(zi[i] * idx)));
       ii = guard_face(s, ii); jj = guard_face(s, jj); kk = guard_face(s, kk);
-      AT(ax, s, ii + 1, jj, kk) += x_l * ru[i];
-      AT(ax, s, ii, jj, kk) += (1 - x_l) * ru[i];
-      AT(ay, s, ii, jj + 1, kk) += y_l * rv[i];
-      AT(ay, s, ii, jj, kk) += (1 - y_l) * rv[i];
-      AT(az, s, ii, jj, kk + 1) += z_l * rw[i];
-      AT(az, s, ii, jj, kk) += (1 - z_l) * rw[i];
+      double r0 = ru[i], r1 = rv[i], r2 = rw[i];
+      if (s->prop[PR_MASS]) {
+        const double m = prop_or(s, PR_MASS, i, 1.0);
+        r0 *= m; r1 *= m; r2 *= m;
+      }
+      AT(ax, s, ii + 1, jj, kk) += x_l * r0;
+      AT(ax, s, ii, jj, kk) += (1 - x_l) * r0;
+      AT(ay, s, ii, jj + 1, kk) += y_l * r1;
+      AT(ay, s, ii, jj, kk) += (1 - y_l) * r1;
+      AT(az, s, ii, jj, kk + 1) += z_l * r2;
+      AT(az, s, ii, jj, kk) += (1 - z_l) * r2;
     }
     fold_cum(s, ax); fold_cum(s, ay); fold_cum(s, az);
     refresh(s, ax); refresh(s, ay); refresh(s, az);

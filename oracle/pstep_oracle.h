@@ -40,6 +40,14 @@ void pso_destroy(pso_state *s);
 /* particle.cpp load_random/Load_All stand-in: set x,u,T,flag for n particles */
 int pso_load(pso_state *s, int64_t n, const double *x, const double *y, const double *z, const double *u,
              const double *v, const double *w, const double *t, const int32_t *flag);
+/* Per-particle properties (no reference counterpart; the library's
+ * pstep_set_particle_props): arrays indexed by particle id (flag, 0..n-1), so
+ * they follow each particle through the reference's reordering; NULL keeps the
+ * scalar. tau_p replaces Tp, mass_ratio weights the momentum deposit, itth
+ * replaces Nu*PI*Dp*k, heat_is 1/(mp*Cvp), alpha the absorbed power, accel
+ * ParticleGravity*g. Call after pso_load. */
+int pso_set_props(pso_state *s, int64_t n, const double *tau_p, const double *mass_ratio, const double *itth,
+                  const double *heat_is, const double *alpha, const double *ax, const double *ay, const double *az);
 /* grid.cpp:207-226: *_int = *_np1 = base; gas2part_Temp_int; Compute_RHS_Temp_int; part2gas_Temp_int -> e */
 int pso_prime(pso_state *s, const double *tfield, double *e);
 /* grid.cpp:659-680 for RK4 stage k with fixed ghosted fields; deposits into c, ax/ay/az, e ((n+2)^3 each) */

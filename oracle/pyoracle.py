@@ -74,6 +74,7 @@ def _load():
         lib.pso_destroy.argtypes = [C.c_void_p]
         lib.pso_load.argtypes = [C.c_void_p, C.c_int64] + [_D] * 7 + [C.POINTER(C.c_int32)]
         lib.pso_prime.argtypes = [C.c_void_p, _D, _D]
+        lib.pso_set_props.argtypes = [C.c_void_p, C.c_int64] + [_D] * 8
         lib.pso_stage.argtypes = [C.c_void_p, C.c_int] + [_D] * 4 + [_D] * 5
         lib.pso_end_stage.argtypes = [C.c_void_p]
         lib.pso_end_step.argtypes = [C.c_void_p]
@@ -117,6 +118,18 @@ class Oracle:
         fl = np.ascontiguousarray(flag, dtype=np.int32)
         rc = _lib.pso_load(self.h, len(fl), *[_p(a) for a in arrs], fl.ctypes.data_as(C.POINTER(C.c_int32)))
         assert rc == 0
+
+    PROPS = ("tau_p", "mass_ratio", "itth", "heat_is", "alpha", "ax", "ay", "az")
+
+    def set_props(self, n, **props):
+        """per-particle properties indexed by particle id (flag); omitted ones keep the scalar"""
+        unknown = set(props) - set(self.PROPS)
+        if unknown:
+            raise ValueError(f"unknown properties {unknown}")
+        self._props = [None if props.get(k) is None else np.ascontiguousarray(props[k], dtype=np.float64)
+                       for k in self.PROPS]
+        ptrs = [None if a is None else _p(a) for a in self._props]
+        assert _lib.pso_set_props(self.h, int(n), *ptrs) == 0
 
     def prime(self, tfield_g):
         _lib.pso_prime(self.h, _p(tfield_g), _p(self.fields["E"]))
@@ -221,3 +234,142 @@ def run_ref(bp, case: dict, nsteps: int, dump_all: bool = True, timing: bool = F
             os.remove(os.path.join(d, f))
         os.rmdir(d)
     return recs, r.stdout
+
+
+# ---------------------------------------------------------------- gas step
+GAS_REF_BIN = os.path.join(HERE, "_ref", "gas_harness")
+GAS_FIELDS = ["RU_x", "RU_y", "RU_z", "Rho", "P", "T", "U_x", "U_y", "U_z", "C", "RHS_RU_x", "RHS_RU_y", "RHS_RU_z",
+              "RHS_Part_Temp", "divergence", "Rho_new"]
+GAS_REC_FIELDS = ["RU_x", "RU_y", "RU_z", "Rho", "P", "T", "RHS_Part_Temp", "C", "RHS_RU_x", "RHS_RU_y", "RHS_RU_z"]
+
+
+class _GasCfg(C.Structure):
+    _fields_ = [("n", C.c_int32), ("cooling", C.c_int32), ("iterations", C.c_int32), ("twc", C.c_int32),
+                ("l", C.c_double), ("dt", C.c_double), ("mu0", C.c_double), ("k", C.c_double), ("cp", C.c_double),
+                ("cv", C.c_double), ("rho0", C.c_double), ("u0", C.c_double), ("a_force", C.c_double),
+                ("gx", C.c_double), ("gy", C.c_double), ("gz", C.c_double), ("mp", C.c_double),
+                ("epsilon", C.c_double)]
+
+
+def _gas_lib():
+    lib = _load()
+    if not getattr(lib, "_gas", False):
+        lib.pgo_create.restype = C.c_void_p
+        lib.pgo_create.argtypes = [C.POINTER(_GasCfg), C.c_void_p]
+        lib.pgo_destroy.argtypes = [C.c_void_p]
+        lib.pgo_init.argtypes = [C.c_void_p] + [_D] * 4 + [C.c_double]
+        lib.pgo_step.argtypes = [C.c_void_p]
+        lib.pgo_field.restype = _D
+        lib.pgo_field.argtypes = [C.c_void_p, C.c_int]
+        lib.pgo_scalar.restype = C.c_double
+        lib.pgo_scalar.argtypes = [C.c_void_p, C.c_int]
+        lib.gas_fft3d.argtypes = [_D, C.c_int, C.c_int]
+        lib._gas = True
+    return lib
+
+
+class GasOracle:
+    """The C restatement of the box gas step (oracle/gas_oracle.c), optionally
+    coupled to a particle-step Oracle (which it drives)."""
+
+    def __init__(self, gcfg: dict, particles: "Oracle | None" = None):
+        lib = _gas_lib()
+        c = _GasCfg()
+        for k in ("n", "cooling", "iterations", "twc"):
+            setattr(c, k, int(gcfg[k]))
+        for k in ("l", "dt", "mu0", "k", "cp", "cv", "rho0", "u0", "a_force", "gx", "gy", "gz", "mp", "epsilon"):
+            setattr(c, k, float(gcfg[k]))
+        self.n = int(gcfg["n"])
+        self.particles = particles
+        self.h = lib.pgo_create(C.byref(c), particles.h if particles is not None else None)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.pgo_destroy(self.h)
+            self.h = None
+
+    def init(self, ru_x, ru_y, ru_z, rho, p0):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (ru_x, ru_y, ru_z, rho)]
+        assert _lib.pgo_init(self.h, *[_p(a) for a in arrs], float(p0)) == 0
+
+    def step(self):
+        assert _lib.pgo_step(self.h) == 0
+
+    def field(self, name: str) -> np.ndarray:
+        g = self.n + 2
+        p = _lib.pgo_field(self.h, GAS_FIELDS.index(name))
+        return np.ctypeslib.as_array(p, shape=(g, g, g)).copy()
+
+    def p0(self) -> float:
+        return float(_lib.pgo_scalar(self.h, 0))
+
+    def iterations(self) -> int:
+        return int(_lib.pgo_scalar(self.h, 3))
+
+
+def fft3d(data: np.ndarray, sign: int) -> np.ndarray:
+    """oracle's radix-2 complex FFT on an (n, n, n) complex array (copy)."""
+    a = np.ascontiguousarray(data, dtype=np.complex128).copy()
+    _gas_lib().gas_fft3d(a.ctypes.data_as(_D), a.shape[0], int(sign))
+    return a
+
+
+def build_gas_ref() -> str | None:
+    if not ref_available():
+        return None
+    r = subprocess.run(["make", "-s", "-C", HERE, "gasref", f"REFDIR={REFDIR}"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference gas build failed:\n" + r.stdout + r.stderr)
+    return GAS_REF_BIN
+
+
+def run_gas_ref(bp, fields: dict, particles: dict, nsteps: int, p0: float) -> list[dict]:
+    """Run the reference's own box gas step (oracle/_ref/gas_harness). fields: interior
+    RU_x, RU_y, RU_z, Rho; particles: x y z u v w t flag."""
+    if not os.path.exists(GAS_REF_BIN):
+        if build_gas_ref() is None:
+            raise RuntimeError("reference sources are not available here")
+    d = tempfile.mkdtemp(prefix="pstep_gasref_")
+    try:
+        pfile = os.path.join(d, "params.in")
+        with open(pfile, "w") as f:
+            f.write(bp.params_file())
+        ifile = os.path.join(d, "input.bin")
+        n = len(particles["flag"])
+        with open(ifile, "wb") as f:
+            f.write(np.int64(n).tobytes())
+            f.write(np.int32(bp.n).tobytes())
+            f.write(np.float64(p0).tobytes())
+            for k in ("RU_x", "RU_y", "RU_z", "Rho"):
+                f.write(np.ascontiguousarray(fields[k], dtype=np.float64).tobytes())
+            for k in ("x", "y", "z", "u", "v", "w", "t"):
+                f.write(np.ascontiguousarray(particles[k], dtype=np.float64).tobytes())
+            f.write(np.ascontiguousarray(particles["flag"], dtype=np.int32).tobytes())
+        ofile = os.path.join(d, "output.bin")
+        r = subprocess.run([GAS_REF_BIN, pfile, ifile, ofile, str(nsteps)], capture_output=True, text=True, cwd=d)
+        if r.returncode != 0:
+            raise RuntimeError("gas_harness failed:\n" + r.stdout + r.stderr)
+        raw = open(ofile, "rb").read()
+    finally:
+        for f in os.listdir(d):
+            os.remove(os.path.join(d, f))
+        os.rmdir(d)
+    g = bp.n + 2
+    g3 = g ** 3
+    recs, off = [], 0
+    while off < len(raw):
+        step, np_ = np.frombuffer(raw, dtype=np.int32, count=2, offset=off)
+        off += 8
+        rec = {"step": int(step), "np": int(np_)}
+        for nm in GAS_REC_FIELDS:
+            rec[nm] = np.frombuffer(raw, dtype=np.float64, count=g3, offset=off).reshape(g, g, g).copy()
+            off += 8 * g3
+        rec["P0"] = float(np.frombuffer(raw, dtype=np.float64, count=1, offset=off)[0])
+        off += 12
+        for nm in ("x", "y", "z", "u", "v", "w", "T"):
+            rec[nm] = np.frombuffer(raw, dtype=np.float64, count=np_, offset=off).copy()
+            off += 8 * np_
+        rec["flag"] = np.frombuffer(raw, dtype=np.int32, count=np_, offset=off).copy()
+        off += 4 * np_
+        recs.append(rec)
+    return recs
