@@ -31,7 +31,7 @@ CU_UNITS = {
     "deposit.cu": ["-fmad=false"],
     "order.cu": ["-fmad=true"],
     "mlp.cu": ["-fmad=true"],
-    "gas.cu": ["-fmad=true"],
+    "gas.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
 }
 

@@ -8,7 +8,7 @@ import subprocess
 import pytest
 
 import helpers  # noqa: F401  (sets sys.path)
-from first_repo_gb300 import _lib, mlp, pstep
+from first_repo_gb300 import _lib, gas, mlp, pstep
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -42,6 +42,15 @@ def test_mlp_header_matches_binding_and_exports(built_cuda):
     exported = set(re.findall(r"\b(pmlp_[a-z0-9_]+)\b", out))
     for name in names:
         assert hasattr(lib, name), name
+        assert name in exported, name
+
+
+def test_gas_header_matches_binding_and_exports(built_cuda):
+    names = declared("pstep_gas.h", "pgas_")
+    assert set(gas.EXPORTS) == set(names)
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.path("libpstep.so")], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\b(pgas_[a-z0-9_]+)\b", out))
+    for name in names:
         assert name in exported, name
 
 

@@ -13,6 +13,9 @@ from first_repo_gb300 import gen
 def gas_case(n, count, seed, cooling=0):
     bp = helpers.make_bp(n, count)
     bp.cooling = cooling
+    # keep the explicit viscous step stable: nu*dt/dx^2 <= 0.05 (box_params derives Mu0 from tau_p,
+    # which for few heavy particles would exceed the RK4 diffusion limit)
+    bp.mu0 = min(bp.mu0, 0.05 * (bp.l / n) ** 2 / bp.dt)
     ux, uy, uz = gen.velocity(n, seed)
     t = gen.temperature(n, seed + 1)
     rho = 1.0 / t

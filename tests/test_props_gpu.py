@@ -62,7 +62,7 @@ def test_fp32_all_properties(built_cuda):
     bp, arrs, fields = _setup(n, count, 2011)
     rng = np.random.default_rng(2012)
     itth0 = bp.nu * np.pi * bp.dp * bp.k
-    is0 = 1.0 / (bp.mp * bp.cvp)
+    is0 = 1.0 / (bp.derived()["mp"] * bp.cvp)
     a0 = 0.25 * bp.epsilonp * np.pi * bp.dp ** 2 * bp.i0
     props = {
         "tau_p": np.exp(rng.uniform(np.log(0.02), np.log(0.5), count)),
