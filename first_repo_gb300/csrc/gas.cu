@@ -651,10 +651,14 @@ int pgas_init(pgas_handle g, pstep_handle h, const double *ru_x, const double *r
   return PSTEP_OK;
 }
 
-int pgas_step(pgas_handle g, pstep_handle h) {
-  if (!g) return PSTEP_ERR_ARG;
+int pgas_stage(pgas_handle g, pstep_handle h, int k) {
+  if (!g || k < 0 || k > 3) return PSTEP_ERR_ARG;
   if (h) GTRY(pstep_set_stream(h, g->stream));
-  for (int k = 0; k < 4; ++k) GTRY(stage(g, h, k));
+  return stage(g, h, k);
+}
+
+int pgas_end_step(pgas_handle g, pstep_handle h) {
+  if (!g) return PSTEP_ERR_ARG;
   Ops o(g);
   // Correct_mean_RU (grid.cpp:566-572, box)
   for (int a = 0; a < 3; ++a) o.mean_zero(o.F(F_RU_NP1 + a));
@@ -666,6 +670,12 @@ int pgas_step(pgas_handle g, pstep_handle h) {
   if (h) GTRY(pstep_end_step(h));
   GCUDA(g, cudaGetLastError());
   return PSTEP_OK;
+}
+
+int pgas_step(pgas_handle g, pstep_handle h) {
+  if (!g) return PSTEP_ERR_ARG;
+  for (int k = 0; k < 4; ++k) GTRY(pgas_stage(g, h, k));
+  return pgas_end_step(g, h);
 }
 
 int pgas_get_field(pgas_handle g, int id, double *dst, int on_device) {

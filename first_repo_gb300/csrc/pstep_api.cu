@@ -57,6 +57,7 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
                const double *w, const double *t, int on_device);
 int f32_set_tau(pstep_ctx *h, const double *tau, int on_device);
 int f32_set_props(pstep_ctx *h, const pstep_particle_props *props, int on_device);
+int f32_set_correction(pstep_ctx *h, const pstep_correction *c);
 int f32_bind_fields(pstep_ctx *h);
 int f32_prime(pstep_ctx *h);
 int f32_stage(pstep_ctx *h, int k, double pre, double post);
@@ -398,6 +399,12 @@ int pstep_set_particle_props(pstep_handle h, const pstep_particle_props *props, 
       props->accel[2])
     return fail(h, PSTEP_ERR_CONFIG, "per-particle properties other than tau_p need the FP32 form");
   return pstep_set_tau_p(h, props->tau_p, on_device);
+}
+
+int pstep_set_correction(pstep_handle h, const pstep_correction *c) {
+  if (!h) return PSTEP_ERR_ARG;
+  if (!is_f32(h)) return c ? fail(h, PSTEP_ERR_CONFIG, "the learned correction needs the FP32 form") : PSTEP_OK;
+  return f32_set_correction(h, c);
 }
 
 int pstep_bind_velocity(pstep_handle h, const double *ux, const double *uy, const double *uz, int on_device) {

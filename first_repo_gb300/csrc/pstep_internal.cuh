@@ -78,6 +78,8 @@ struct pstep_ctx {
   int64_t np;
   int64_t cap;
   int num_sms;
+  int corr_on;                              // learned correction active (FP32 form)
+  alignas(16) unsigned char corr_dev[256];  // its kernel constants (stage_f32.cu)
 
   // FP64 state
   pstep::F64State s;

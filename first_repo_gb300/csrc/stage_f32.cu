@@ -30,8 +30,10 @@
 // FP64 on GB300 runs at a small fraction of the fp32 rate, so this form keeps
 // fp64 out of every per-particle operation: the only fp64 arithmetic left is
 // the balance reduction over the grid.
+#include <cuda_bf16.h>
 #include <stdlib.h>
 #include "pstep_internal.cuh"
+#include "tc05.cuh"
 
 namespace pstep {
 int interior_mean(pstep_ctx *h, const double *f, double *out_dev);
@@ -81,6 +83,7 @@ struct F32Form {
   float *itp;      // per-particle 1/tau_p or nullptr
   float *pp[7];    // per-particle mass ratio, itth, 1/(m Cvp), alpha, body acceleration x y z (or nullptr)
   float *gas[4];   // ug vg wg at x_int and Tg - t_ref at x_new of the last stage (PSTEP_KEEP_GAS)
+  float *drive[4]; // learned correction: the slip (3) and T_new - Tg the last stage's drag and heat transfer used
   float *rhs_u[3];
   float *uf[3], *tf;  // fp32 ghosted copies of the bound fields
   uint32_t *key;      // brick-major cell id of the base position
@@ -92,6 +95,7 @@ struct F32Form {
   int32_t *se;        // fixed-point scale exponents per field
   Work work;
   int launch_no;      // deposit launches since the last work-list build (counter index)
+  void *corr_mem;     // learned correction: packed weight image + biases (device), or nullptr
   int sorted;
   int tref_set;
   double tref;        // temperature reference (see above)
@@ -157,9 +161,151 @@ struct C32 {
   float dt_pre, dt_post, dt_pre_is, dt_post_is;
   float dpre_idx[3], dpost_idx[3];  // dt*pre/dx, dt*post/dx per dimension
   float itp, g[3], alpha, itth;
+  float is;  // 1/(mp*Cvp) (particle.cpp:485)
 };
 
 enum { PP_MASS = 0, PP_ITTH, PP_HEAT_IS, PP_ALPHA, PP_ACC };  // F32Form::pp slots (PP_ACC + d)
+
+// learned correction: the drive slip / temperature difference at most 10x the plain one
+constexpr float kDriveCap = 10.f;
+
+// One particle's stage: everything the advance kernels read, and the gas velocity
+// interpolated at x_int (particle.cpp:340-360).
+struct Adv {
+  uint32_t cb, cint, cacc;
+  float ob[3], oin[3], oac[3], vb[4], vin[4], vac[4];
+  float rhs_t_old, itp, itth, alpha, dpre_is, dpost_is, gacc[3];
+  float gas[3];
+};
+
+template <int K>
+__device__ __forceinline__ void adv_load(const Geom &G, const F32Form &f, const C32 &c, int64_t p, Adv &a) {
+  const Set32 &B = f.set[SBASE];
+  const Set32 &I = (K == 0) ? f.set[SBASE] : f.set[SINT];
+  const Set32 &A = (K == 0) ? f.set[SBASE] : f.set[SNP1];
+  a.cb = B.cell[p];
+  a.cint = I.cell[p];
+  a.cacc = A.cell[p];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) { a.ob[d] = B.o[d][p]; a.oin[d] = I.o[d][p]; a.oac[d] = A.o[d][p]; }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) { a.vb[q] = B.v[q][p]; a.vin[q] = I.v[q][p]; a.vac[q] = A.v[q][p]; }
+  a.rhs_t_old = f.rhs_t[p];
+  a.itp = f.itp ? f.itp[p] : c.itp;
+  a.itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
+  a.alpha = f.pp[PP_ALPHA] ? f.pp[PP_ALPHA][p] : c.alpha;
+  a.dpre_is = f.pp[PP_HEAT_IS] ? c.dt_pre * f.pp[PP_HEAT_IS][p] : c.dt_pre_is;
+  a.dpost_is = f.pp[PP_HEAT_IS] ? c.dt_post * f.pp[PP_HEAT_IS][p] : c.dt_post_is;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) a.gacc[d] = f.pp[PP_ACC + d] ? f.pp[PP_ACC + d][p] : c.g[d];
+  // face-normal interpolation at x_int (particle.cpp:340-360)
+  const int ii = ci_(a.cint) + 1, jj = cj_(a.cint) + 1, kk = ck_(a.cint) + 1;
+  const float xl = a.oin[0], yl = a.oin[1], zl = a.oin[2];
+  a.gas[0] = xl * f.uf[0][glin3(G, ii + 1, jj, kk)] + (1.f - xl) * f.uf[0][glin3(G, ii, jj, kk)];
+  a.gas[1] = yl * f.uf[1][glin3(G, ii, jj + 1, kk)] + (1.f - yl) * f.uf[1][glin3(G, ii, jj, kk)];
+  a.gas[2] = zl * f.uf[2][glin3(G, ii, jj, kk + 1)] + (1.f - zl) * f.uf[2][glin3(G, ii, jj, kk)];
+}
+
+// The rest of the stage for one particle, with a.gas the gas velocity to use; with
+// ty != 0 the interpolated gas temperature Tg is replaced by Tg - ty * dT, dT the
+// previous stage's T_new - Tg (td_prev, or the current T_new - Tg when there is
+// none): the learned correction of the particle's own heating. Returns the
+// T_new - Tg the heat transfer used.
+template <int K>
+__device__ __forceinline__ float adv_finish_t(const Geom &G, const F32Form &f, const C32 &c, int twc, int64_t p, Adv &a,
+                                              float ty, float td_prev, int32_t *__restrict__ err, float &mu0, float &mu1,
+                                              float &mu2, float &mt) {
+  // positions (particle.cpp:314-338) in cell units
+  int ia[3] = {ci_(a.cacc), cj_(a.cacc), ck_(a.cacc)};
+  int ib[3] = {ci_(a.cb), cj_(a.cb), ck_(a.cb)};
+  int in_[3];
+  float on[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    a.oac[d] += c.dpost_idx[d] * a.vin[d];
+    renorm(ia[d], a.oac[d], G.n[d]);
+    if (K != 3) {
+      on[d] = a.ob[d] + c.dpre_idx[d] * a.vin[d];
+      in_[d] = ib[d];
+      renorm(in_[d], on[d], G.n[d]);
+    } else {
+      on[d] = a.oac[d];
+      in_[d] = ia[d];
+    }
+  }
+  // velocity and temperature (particle.cpp:362-399, 480-496)
+  float rhs[3], vn[4];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    rhs[d] = (a.gas[d] - a.vin[d]) * a.itp;
+    a.vac[d] += c.dt_post * (rhs[d] + a.gacc[d]);
+    vn[d] = (K != 3) ? a.vb[d] + c.dt_pre * (rhs[d] + a.gacc[d]) : a.vac[d];
+  }
+  a.vac[3] += a.dpost_is * (a.rhs_t_old + a.alpha);
+  vn[3] = (K != 3) ? a.vb[3] + a.dpre_is * (a.rhs_t_old + a.alpha) : a.vac[3];
+
+  // trilinear T at x_new (particle.cpp:430-456): node = cell + h, x_l = o - h + 1/2
+  const int hx = on[0] >= 0.5f, hy = on[1] >= 0.5f, hz = on[2] >= 0.5f;
+  const int ni = in_[0] + hx + 1, nj = in_[1] + hy + 1, nk = in_[2] + hz + 1;  // ghosted node
+  const float *T = f.tf;
+  const float wx = on[0] - hx + 0.5f, wy = on[1] - hy + 0.5f, wz = on[2] - hz + 0.5f;
+  float tg = wx * wy * wz * T[glin3(G, ni, nj, nk)] + (1.f - wx) * wy * wz * T[glin3(G, ni - 1, nj, nk)] +
+             wx * (1.f - wy) * wz * T[glin3(G, ni, nj - 1, nk)] + wx * wy * (1.f - wz) * T[glin3(G, ni, nj, nk - 1)] +
+             (1.f - wx) * (1.f - wy) * wz * T[glin3(G, ni - 1, nj - 1, nk)] +
+             (1.f - wx) * wy * (1.f - wz) * T[glin3(G, ni - 1, nj, nk - 1)] +
+             wx * (1.f - wy) * (1.f - wz) * T[glin3(G, ni, nj - 1, nk - 1)] +
+             (1.f - wx) * (1.f - wy) * (1.f - wz) * T[glin3(G, ni - 1, nj - 1, nk - 1)];
+  if (ty != 0.f) {
+    const float dtn = vn[3] - tg;
+    const float cap = kDriveCap * fabsf(dtn);
+    const float td = td_prev != 0.f ? (fabsf(td_prev) <= cap ? td_prev : copysignf(cap, td_prev)) : dtn;
+    tg -= ty * td;
+  }
+  const float rhs_t_new = (tg - vn[3]) * a.itth;
+  if (!isfinite(rhs_t_new) || !isfinite(vn[0]) || !isfinite(vn[1]) || !isfinite(vn[2]) || !isfinite(on[0]) ||
+      !isfinite(on[1]) || !isfinite(on[2]))
+    atomicOr(err, kErrNonFinite);
+
+  // stores
+  const Set32 &N = f.set[SNEW];
+  const Set32 &P = f.set[SNP1];
+  N.cell[p] = pack(in_[0], in_[1], in_[2]);
+  P.cell[p] = pack(ia[0], ia[1], ia[2]);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) { N.o[d][p] = on[d]; P.o[d][p] = a.oac[d]; }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) { N.v[q][p] = vn[q]; P.v[q][p] = a.vac[q]; }
+  // the momentum deposit carries the particle's mass relative to cfg.mp
+  const float mrel = f.pp[PP_MASS] ? f.pp[PP_MASS][p] : 1.f;
+  if (twc) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) f.rhs_u[d][p] = rhs[d] * mrel;
+  }
+  f.rhs_t[p] = rhs_t_new;
+  if (f.gas[0]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) f.gas[d][p] = a.gas[d];
+    f.gas[3][p] = tg;
+  }
+  mu0 = fmaxf(mu0, fabsf(rhs[0] * mrel));
+  mu1 = fmaxf(mu1, fabsf(rhs[1] * mrel));
+  mu2 = fmaxf(mu2, fabsf(rhs[2] * mrel));
+  mt = fmaxf(mt, fabsf(rhs_t_new));
+  return vn[3] - tg;
+}
+
+template <int K>
+__device__ __forceinline__ void adv_finish(const Geom &G, const F32Form &f, const C32 &c, int twc, int64_t p, Adv &a,
+                                           int32_t *__restrict__ err, float &mu0, float &mu1, float &mu2, float &mt) {
+  (void)adv_finish_t<K>(G, f, c, twc, p, a, 0.f, 0.f, err, mu0, mu1, mu2, mt);
+}
+
+template <int K>
+__device__ __forceinline__ float adv_finish_mlp(const Geom &G, const F32Form &f, const C32 &c, int twc, int64_t p,
+                                                Adv &a, float ty, float td_prev, int32_t *__restrict__ err, float &mu0,
+                                                float &mu1, float &mu2, float &mt) {
+  return adv_finish_t<K>(G, f, c, twc, p, a, ty, td_prev, err, mu0, mu1, mu2, mt);
+}
 
 template <int K>
 __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int twc, int64_t n,
@@ -167,105 +313,237 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
   if (p < n) {
-    const Set32 &B = f.set[SBASE];
-    const Set32 &I = (K == 0) ? f.set[SBASE] : f.set[SINT];
-    const Set32 &A = (K == 0) ? f.set[SBASE] : f.set[SNP1];
-    const uint32_t cb = B.cell[p];
-    const uint32_t cint = I.cell[p];
-    uint32_t cacc = A.cell[p];
-    float ob[3], oin[3], oac[3], vb[4], vin[4], vac[4];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) { ob[d] = B.o[d][p]; oin[d] = I.o[d][p]; oac[d] = A.o[d][p]; }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) { vb[q] = B.v[q][p]; vin[q] = I.v[q][p]; vac[q] = A.v[q][p]; }
-    const float rhs_t_old = f.rhs_t[p];
-    const float itp = f.itp ? f.itp[p] : c.itp;
-    const float itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
-    const float alpha = f.pp[PP_ALPHA] ? f.pp[PP_ALPHA][p] : c.alpha;
-    const float dpre_is = f.pp[PP_HEAT_IS] ? c.dt_pre * f.pp[PP_HEAT_IS][p] : c.dt_pre_is;
-    const float dpost_is = f.pp[PP_HEAT_IS] ? c.dt_post * f.pp[PP_HEAT_IS][p] : c.dt_post_is;
-    float gacc[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) gacc[d] = f.pp[PP_ACC + d] ? f.pp[PP_ACC + d][p] : c.g[d];
-
-    // face-normal interpolation at x_int (particle.cpp:340-360)
-    const int ii = ci_(cint) + 1, jj = cj_(cint) + 1, kk = ck_(cint) + 1;
-    const float xl = oin[0], yl = oin[1], zl = oin[2];
-    const float ug = xl * f.uf[0][glin3(G, ii + 1, jj, kk)] + (1.f - xl) * f.uf[0][glin3(G, ii, jj, kk)];
-    const float vg = yl * f.uf[1][glin3(G, ii, jj + 1, kk)] + (1.f - yl) * f.uf[1][glin3(G, ii, jj, kk)];
-    const float wg = zl * f.uf[2][glin3(G, ii, jj, kk + 1)] + (1.f - zl) * f.uf[2][glin3(G, ii, jj, kk)];
-    const float gas[3] = {ug, vg, wg};
-
-    // positions (particle.cpp:314-338) in cell units
-    int ia[3] = {ci_(cacc), cj_(cacc), ck_(cacc)};
-    int ib[3] = {ci_(cb), cj_(cb), ck_(cb)};
-    int in_[3];
-    float on[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      oac[d] += c.dpost_idx[d] * vin[d];
-      renorm(ia[d], oac[d], G.n[d]);
-      if (K != 3) {
-        on[d] = ob[d] + c.dpre_idx[d] * vin[d];
-        in_[d] = ib[d];
-        renorm(in_[d], on[d], G.n[d]);
-      } else {
-        on[d] = oac[d];
-        in_[d] = ia[d];
-      }
-    }
-    // velocity and temperature (particle.cpp:362-399, 480-496)
-    float rhs[3], vn[4];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      rhs[d] = (gas[d] - vin[d]) * itp;
-      vac[d] += c.dt_post * (rhs[d] + gacc[d]);
-      vn[d] = (K != 3) ? vb[d] + c.dt_pre * (rhs[d] + gacc[d]) : vac[d];
-    }
-    vac[3] += dpost_is * (rhs_t_old + alpha);
-    vn[3] = (K != 3) ? vb[3] + dpre_is * (rhs_t_old + alpha) : vac[3];
-
-    // trilinear T at x_new (particle.cpp:430-456): node = cell + h, x_l = o - h + 1/2
-    const int hx = on[0] >= 0.5f, hy = on[1] >= 0.5f, hz = on[2] >= 0.5f;
-    const float tx = on[0] - hx + 0.5f, ty = on[1] - hy + 0.5f, tz = on[2] - hz + 0.5f;
-    const int ni = in_[0] + hx + 1, nj = in_[1] + hy + 1, nk = in_[2] + hz + 1;  // ghosted node
-    const float *T = f.tf;
-    const float tg = tx * ty * tz * T[glin3(G, ni, nj, nk)] + (1.f - tx) * ty * tz * T[glin3(G, ni - 1, nj, nk)] +
-                     tx * (1.f - ty) * tz * T[glin3(G, ni, nj - 1, nk)] + tx * ty * (1.f - tz) * T[glin3(G, ni, nj, nk - 1)] +
-                     (1.f - tx) * (1.f - ty) * tz * T[glin3(G, ni - 1, nj - 1, nk)] +
-                     (1.f - tx) * ty * (1.f - tz) * T[glin3(G, ni - 1, nj, nk - 1)] +
-                     tx * (1.f - ty) * (1.f - tz) * T[glin3(G, ni, nj - 1, nk - 1)] +
-                     (1.f - tx) * (1.f - ty) * (1.f - tz) * T[glin3(G, ni - 1, nj - 1, nk - 1)];
-    const float rhs_t_new = (tg - vn[3]) * itth;
-    if (!isfinite(rhs_t_new) || !isfinite(vn[0]) || !isfinite(vn[1]) || !isfinite(vn[2]) || !isfinite(on[0]) ||
-        !isfinite(on[1]) || !isfinite(on[2]))
-      atomicOr(err, kErrNonFinite);
-
-    // stores
-    const Set32 &N = f.set[SNEW];
-    const Set32 &P = f.set[SNP1];
-    N.cell[p] = pack(in_[0], in_[1], in_[2]);
-    P.cell[p] = pack(ia[0], ia[1], ia[2]);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) { N.o[d][p] = on[d]; P.o[d][p] = oac[d]; }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) { N.v[q][p] = vn[q]; P.v[q][p] = vac[q]; }
-    // the momentum deposit carries the particle's mass relative to cfg.mp
-    const float mrel = f.pp[PP_MASS] ? f.pp[PP_MASS][p] : 1.f;
-    if (twc) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) f.rhs_u[d][p] = rhs[d] * mrel;
-    }
-    f.rhs_t[p] = rhs_t_new;
-    if (f.gas[0]) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) f.gas[d][p] = gas[d];
-      f.gas[3][p] = tg;
-    }
-    mu0 = rhs[0] * mrel; mu1 = rhs[1] * mrel; mu2 = rhs[2] * mrel; mt = rhs_t_new;
+    Adv a;
+    adv_load<K>(G, f, c, p, a);
+    adv_finish<K>(G, f, c, twc, p, a, err, mu0, mu1, mu2, mt);
   }
   // bounds for the fixed-point scales (order-independent maxima)
-  block_max4(f.slots, fabsf(mu0), fabsf(mu1), fabsf(mu2), fabsf(mt));
+  block_max4(f.slots, mu0, mu1, mu2, mt);
+}
+
+// ----------------------------------------------------------------------------
+// The learned correction fused into the advance (pstep_set_correction).
+//
+// Persistent CTAs of 128 threads, one particle per thread and tile of 128
+// particles; thread t's network row is tensor-memory lane t. Per tile: plain
+// interpolation and features in registers, the feature row as bf16 to shared
+// memory, three tcgen05 MMAs (16 -> 64 -> 64 -> 16 columns, accumulators in
+// tensor memory, bias and SiLU between them in registers), then the corrected
+// gas velocity and temperature feed the same finish as the plain step.
+// Particles outside the training ranges keep the plain interpolation.
+namespace corr {
+constexpr int kRows = 128, kInP = 16, kHid = 64, kOutP = 16;
+constexpr uint32_t W1 = 0, W2 = W1 + kHid * kInP * 2, W3 = W2 + kHid * kHid * 2, XA = W3 + kOutP * kHid * 2,
+                   H1A = XA + kRows * kInP * 2, H2A = H1A + kRows * kHid * 2, BIAS = H2A + kRows * kHid * 2,
+                   MISC = BIAS + (kHid + kHid + kOutP) * 4, kBytes = MISC + 64;
+constexpr uint32_t kImage = XA;  // packed weight image: W1 | W2 | W3 tiles, bf16
+// at most 4 CTAs fit on an SM, so 4 x 128 tensor-memory columns never exceed 512
+constexpr uint32_t kAlloc = 52 * 1024;
+static_assert(kBytes <= kAlloc, "correction smem");
+constexpr uint32_t kWaitLimit = 1u << 22;
+}  // namespace corr
+
+struct CorrDev {
+  const uint4 *image;  // kImage bytes
+  const float *bias;   // b1[64] b2[64] b3[16]
+  float shift[10], scale[10], lo[4], hi[4];
+  float inv_nu;        // 1 / kinematic viscosity of the gas
+  float inv_prior_re;  // 1 / prior_re (0: outputs not scaled by the prior)
+  float dp_per_itth;   // d_p = itth * dp_per_itth (1 / (Nu PI k)), per-particle diameters
+  float dp;            // scalar diameter (no per-particle itth)
+  float idx;           // 1 / dx
+};
+
+static_assert(sizeof(CorrDev) <= sizeof(((pstep_ctx *)nullptr)->corr_dev), "correction constants");
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+template <int C>
+__device__ __forceinline__ void corr_row(uint8_t *tile, int r, const float *v) {
+#pragma unroll
+  for (int cb = 0; cb < C / 8; ++cb) {
+    uint4 q;
+    q.x = pack_bf16x2(v[cb * 8 + 0], v[cb * 8 + 1]);
+    q.y = pack_bf16x2(v[cb * 8 + 2], v[cb * 8 + 3]);
+    q.z = pack_bf16x2(v[cb * 8 + 4], v[cb * 8 + 5]);
+    q.w = pack_bf16x2(v[cb * 8 + 6], v[cb * 8 + 7]);
+    *reinterpret_cast<uint4 *>(tile + tc05::tile_off(r, cb * 8, C)) = q;
+  }
+}
+
+__device__ __forceinline__ void corr_sync() {
+  tc05::fence_smem_async();
+  tc05::fence_before();
+  __syncthreads();
+  tc05::fence_after();
+}
+
+__device__ __forceinline__ bool corr_wait(uint64_t *mbar, uint32_t &phase) {
+  const bool ok = tc05::mbar_wait(mbar, phase, corr::kWaitLimit);
+  tc05::fence_after();
+  const bool all = __syncthreads_and(ok ? 1 : 0) != 0;
+  if (all) phase ^= 1u;
+  return all;
+}
+
+template <int K>
+__global__ void __launch_bounds__(128, 4) k_advance32_mlp(Geom G, F32Form f, C32 c, int twc, int64_t n,
+                                                          int32_t *__restrict__ err, CorrDev cd) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  using namespace tc05;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  uint8_t *W1 = sm + corr::W1, *W2 = sm + corr::W2, *W3 = sm + corr::W3, *XA = sm + corr::XA, *H1A = sm + corr::H1A,
+          *H2A = sm + corr::H2A;
+  float *b1 = reinterpret_cast<float *>(sm + corr::BIAS), *b2 = b1 + corr::kHid, *b3 = b2 + corr::kHid;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + corr::MISC);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + corr::MISC + 8);
+  for (uint32_t q = tid; q < corr::kImage / 16; q += corr::kRows) reinterpret_cast<uint4 *>(sm)[q] = cd.image[q];
+  for (int q = tid; q < corr::kHid + corr::kHid + corr::kOutP; q += corr::kRows) b1[q] = cd.bias[q];
+  if (tid == 0) mbar_init(mbar, 1);
+  if (warp == 0) tmem_alloc(tslot, 128);
+  corr_sync();
+  const uint32_t tm = *tslot;
+  const uint32_t tl = tm + ((uint32_t)(warp * 32) << 16);
+  const uint32_t id64 = idesc_bf16(128, 64), id16 = idesc_bf16(128, 16);
+  uint32_t phase = 0;
+  bool ok = true;
+  float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
+  const int64_t ntiles = (n + corr::kRows - 1) / corr::kRows;
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int64_t p = tile * corr::kRows + tid;
+    const bool live = p < n;
+    Adv a;
+    float x[corr::kInP];
+#pragma unroll
+    for (int j = 0; j < corr::kInP; ++j) x[j] = 0.f;
+    float smag = 0.f, sdrv = 0.f, prior = 1.f;
+    bool use = false;
+    if (live) {
+      adv_load<K>(G, f, c, p, a);
+      // features (pstep.h, pstep_correction) from the slip that drives the drag: the previous
+      // stage's (at most kDriveCap x the plain slip), or the plain slip when there is none
+      float s0 = a.vin[0] - a.gas[0], s1 = a.vin[1] - a.gas[1], s2 = a.vin[2] - a.gas[2];
+      smag = sqrtf(s0 * s0 + s1 * s1 + s2 * s2);
+      const float d0 = f.drive[0][p], d1 = f.drive[1][p], d2 = f.drive[2][p];
+      const float dmag = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+      sdrv = smag;
+      if (dmag > 0.f) {
+        sdrv = fminf(dmag, kDriveCap * smag);
+        s0 = d0;
+        s1 = d1;
+        s2 = d2;
+      }
+      const float smagd = dmag > 0.f ? dmag : smag;
+      const float dp = f.pp[PP_ITTH] ? a.itth * cd.dp_per_itth : cd.dp;
+      const float dpdx = dp * cd.idx;
+      const float rep = sdrv * dp * cd.inv_nu;
+      const float his = f.pp[PP_HEAT_IS] ? f.pp[PP_HEAT_IS][p] : c.is;
+      const float q = a.alpha * his;
+      const float taup = 1.f / a.itp;
+      if (cd.inv_prior_re > 0.f) prior = dpdx / (1.f + rep / dpdx * cd.inv_prior_re);
+      use = smag > 0.f && smagd > 0.f && dpdx >= cd.lo[0] && dpdx <= cd.hi[0] && rep >= cd.lo[1] && rep <= cd.hi[1] &&
+            q >= cd.lo[2] && q <= cd.hi[2] && taup >= cd.lo[3] && taup <= cd.hi[3];
+      if (use) {
+        const float inv = 1.f / smagd;
+        const float raw[10] = {a.oin[0], a.oin[1], a.oin[2], s0 * inv, s1 * inv, s2 * inv, dpdx, logf(rep), q,
+                               logf(taup)};
+#pragma unroll
+        for (int j = 0; j < 10; ++j) x[j] = (raw[j] - cd.shift[j]) * cd.scale[j];
+      }
+    }
+    corr_row<corr::kInP>(XA, tid, x);
+    corr_sync();
+    if (tid == 0) {
+      mma_bf16(tm, tile_desc(smem_u32(XA), corr::kInP, 0, 0), tile_desc(smem_u32(W1), corr::kInP, 0, 0), id64, 0);
+      commit(mbar);
+    }
+    ok = corr_wait(mbar, phase);
+    if (!ok) break;
+    {
+      float h[corr::kHid];
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        float v[16];
+        tmem_ld16(tl + cc * 16, v);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const float z = v[q] + b1[cc * 16 + q];
+          h[cc * 16 + q] = z / (1.f + expf(-z));
+        }
+      }
+      corr_row<corr::kHid>(H1A, tid, h);
+    }
+    corr_sync();
+    if (tid == 0) {
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks)
+        mma_bf16(tm + 64, tile_desc(smem_u32(H1A), corr::kHid, 0, ks), tile_desc(smem_u32(W2), corr::kHid, 0, ks), id64, ks);
+      commit(mbar);
+    }
+    ok = corr_wait(mbar, phase);
+    if (!ok) break;
+    {
+      float h[corr::kHid];
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        float v[16];
+        tmem_ld16(tl + 64 + cc * 16, v);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const float z = v[q] + b2[cc * 16 + q];
+          h[cc * 16 + q] = z / (1.f + expf(-z));
+        }
+      }
+      corr_row<corr::kHid>(H2A, tid, h);
+    }
+    corr_sync();
+    if (tid == 0) {  // D3 reuses columns [0, 16): D1 has been read
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks)
+        mma_bf16(tm, tile_desc(smem_u32(H2A), corr::kHid, 0, ks), tile_desc(smem_u32(W3), corr::kHid, 0, ks), id16, ks);
+      commit(mbar);
+    }
+    ok = corr_wait(mbar, phase);
+    if (!ok) break;
+    float y[16];
+    tmem_ld16(tl, y);
+    if (live) {
+      // The network gives the disturbance per unit of the slip (excess temperature) that drove
+      // it, y = d/|s|, learned where the drag used the disturbed slip. Here the drag uses the
+      // corrected slip, so the disturbance is scaled by the slip (temperature difference) the
+      // particle's drag (heat transfer) used in the previous stage: a fixed-point iteration
+      // across stages towards d = y |s_drive|, s_drive = s + d, that leaves the drag's
+      // dependence on the current gas value as in the plain step. The drive is capped at
+      // kDriveCap x the plain value (self-consistent up to k = y . s/|s| = 1 - 1/kDriveCap).
+      float ty = 0.f, tdrive = 0.f;
+      const float td_prev = f.drive[3][p];
+      if (use) {
+        const float y0 = (y[0] + b3[0]) * prior, y1 = (y[1] + b3[1]) * prior, y2 = (y[2] + b3[2]) * prior;
+        a.gas[0] -= sdrv * y0;
+        a.gas[1] -= sdrv * y1;
+        a.gas[2] -= sdrv * y2;
+        ty = (y[3] + b3[3]) * prior;
+        tdrive = td_prev;
+      }
+      f.drive[0][p] = a.vin[0] - a.gas[0];
+      f.drive[1][p] = a.vin[1] - a.gas[1];
+      f.drive[2][p] = a.vin[2] - a.gas[2];
+      f.drive[3][p] = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, tdrive, err, mu0, mu1, mu2, mt);
+    }
+    tc05::fence_before();  // this tile's tensor-memory reads before the next tile's MMAs
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, kErrTimeout);
+    tc05::mbar_wait(mbar, phase, corr::kWaitLimit);
+  }
+  block_max4(f.slots, mu0, mu1, mu2, mt);
+  tc05::fence_before();
+  __syncthreads();
+  tc05::fence_after();
+  if (warp == 0) tmem_dealloc(tm, 128);
 }
 
 // the prime (grid.cpp:223-226) at the base positions: Tg, RHS_T
@@ -741,6 +1019,7 @@ C32 make_c32(const pstep_ctx *h, int k, double pre, double post) {
   c.g[2] = (float)(cfg.particle_gravity * cfg.gz);
   c.alpha = (float)(0.25 * cfg.epsilonp * kPi * cfg.dp * cfg.dp * cfg.i0);
   c.itth = (float)(cfg.nu * kPi * cfg.dp * cfg.k);
+  c.is = (float)iS;
   (void)k;
   return c;
 }
@@ -798,6 +1077,8 @@ int sort_step(pstep_ctx *h) {
       if (f.pp[q]) permf(f.pp[q]);
     for (int q = 0; q < 4; ++q)
       if (f.gas[q]) permf(f.gas[q]);
+    for (int q = 0; q < 4; ++q)
+      if (f.drive[q]) permf(f.drive[q]);
     {
       k_perm<uint32_t><<<nb(n), kThreads, 0, h->stream>>>(B.cell, f.sidx, n, (uint32_t *)f.tmpf);
       uint32_t *t = B.cell; B.cell = (uint32_t *)f.tmpf; f.tmpf = (float *)t;
@@ -897,8 +1178,10 @@ int f32_destroy(pstep_ctx *h) {
     for (int q = 0; q < 4; ++q) dfree32(f->set[s].v[q]);
   }
   dfree32(f->rhs_t); dfree32(f->itp);
+  if (f->corr_mem) cudaFree(f->corr_mem);
   for (int q = 0; q < 7; ++q) dfree32(f->pp[q]);
   for (int q = 0; q < 4; ++q) dfree32(f->gas[q]);
+  for (int q = 0; q < 4; ++q) dfree32(f->drive[q]);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx); dfree32(f->tmpf);
   dfree32(f->bounds); dfree32(f->se); dfree32(f->slots);
@@ -919,6 +1202,8 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
   const int64_t n = h->np;
   dfree32(f.itp);
   for (int q = 0; q < 7; ++q) dfree32(f.pp[q]);
+  for (int q = 0; q < 4; ++q)
+    if (f.drive[q]) PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
   f.sorted = 0;
   if (n == 0) return PSTEP_OK;
   if (!f.tref_set) {
@@ -1014,6 +1299,87 @@ int f32_set_props(pstep_ctx *h, const pstep_particle_props *pr, int on_device) {
   return PSTEP_OK;
 }
 
+// host round-to-nearest-even fp32 -> bf16 bits (finite values)
+static uint16_t bf16_bits(float v) {
+  uint32_t u;
+  memcpy(&u, &v, 4);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
+  F32Form &f = *h->f32;
+  if (f.corr_mem) {
+    PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+    cudaFree(f.corr_mem);
+    f.corr_mem = nullptr;
+  }
+  h->corr_on = 0;
+  if (!pc) return PSTEP_OK;
+  if (!pc->params || !(pc->nu_gas > 0)) {
+    snprintf(h->err, sizeof h->err, "correction needs parameters and a positive gas viscosity");
+    return PSTEP_ERR_ARG;
+  }
+  const Geom &G = h->geom;
+  if (G.n[0] != G.n[1] || G.n[0] != G.n[2] || G.l[0] != G.l[1] || G.l[0] != G.l[2]) {
+    snprintf(h->err, sizeof h->err, "the correction's d_p/dx needs a cubic grid");
+    return PSTEP_ERR_CONFIG;
+  }
+  // weight tiles in the canonical K-major layout (tc05.cuh), then fp32 biases
+  const size_t bias_off = corr::kImage;
+  const size_t bytes = bias_off + sizeof(float) * (corr::kHid + corr::kHid + corr::kOutP);
+  uint8_t *img = (uint8_t *)calloc(1, bytes);
+  const float *P = pc->params;
+  for (int o = 0; o < corr::kHid; ++o)
+    for (int j = 0; j < corr::kInP; ++j)
+      *(uint16_t *)(img + corr::W1 + tc05::tile_off(o, j, corr::kInP)) = bf16_bits(P[o * corr::kInP + j]);
+  for (int o = 0; o < corr::kHid; ++o)
+    for (int i = 0; i < corr::kHid; ++i)
+      *(uint16_t *)(img + corr::W2 + tc05::tile_off(o, i, corr::kHid)) = bf16_bits(P[1088 + o * corr::kHid + i]);
+  for (int o = 0; o < corr::kOutP; ++o)
+    for (int i = 0; i < corr::kHid; ++i)
+      *(uint16_t *)(img + corr::W3 + tc05::tile_off(o, i, corr::kHid)) = bf16_bits(P[5248 + o * corr::kHid + i]);
+  float *bias = (float *)(img + bias_off);
+  for (int q = 0; q < corr::kHid; ++q) bias[q] = P[1024 + q];
+  for (int q = 0; q < corr::kHid; ++q) bias[corr::kHid + q] = P[5184 + q];
+  for (int q = 0; q < corr::kOutP; ++q) bias[2 * corr::kHid + q] = P[6272 + q];
+  cudaError_t e = cudaMalloc(&f.corr_mem, bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(f.corr_mem, img, bytes, cudaMemcpyHostToDevice);
+  free(img);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    f.corr_mem = nullptr;
+    snprintf(h->err, sizeof h->err, "correction upload: %s", cudaGetErrorString(e));
+    return PSTEP_ERR_CUDA;
+  }
+  CorrDev &cd = *reinterpret_cast<CorrDev *>(h->corr_dev);
+  cd.image = (const uint4 *)f.corr_mem;
+  cd.bias = (const float *)((const uint8_t *)f.corr_mem + bias_off);
+  for (int q = 0; q < 10; ++q) { cd.shift[q] = pc->shift[q]; cd.scale[q] = pc->scale[q]; }
+  for (int q = 0; q < 4; ++q) { cd.lo[q] = pc->lo[q]; cd.hi[q] = pc->hi[q]; }
+  cd.inv_nu = (float)(1.0 / pc->nu_gas);
+  cd.inv_prior_re = pc->prior_re > 0.f ? 1.f / pc->prior_re : 0.f;
+  const pstep_config &cfg = h->cfg;
+  cd.dp_per_itth = (cfg.nu > 0 && cfg.k > 0) ? (float)(1.0 / (cfg.nu * kPi * cfg.k)) : 0.f;
+  cd.dp = (float)cfg.dp;
+  cd.idx = (float)G.idx[0];
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_advance32_mlp<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
+    cudaFuncSetAttribute(k_advance32_mlp<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
+    cudaFuncSetAttribute(k_advance32_mlp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
+    cudaFuncSetAttribute(k_advance32_mlp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
+    PSTEP_CUDA(cudaGetLastError());
+    attr = true;
+  }
+  for (int q = 0; q < 4; ++q) {
+    if (!f.drive[q]) TRY32(dalloc32(h, f.drive[q], (size_t)h->cap));
+    PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
+  }
+  h->corr_on = 1;
+  return PSTEP_OK;
+}
+
 int f32_bind_fields(pstep_ctx *h) {
   F32Form &f = *h->f32;
   const int64_t gs = h->geom.gsize;
@@ -1051,7 +1417,20 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
   const C32 c = make_c32(h, k, pre, post);
   const int64_t n = h->np;
   prof_begin(h, PSTEP_PHASE_ADVANCE);
-  if (n > 0) {
+  if (n > 0 && h->corr_on) {
+    // persistent: 4 CTAs per SM (the tensor-memory and shared-memory budget), tiles of 128 particles
+    const CorrDev &cd = *reinterpret_cast<const CorrDev *>(h->corr_dev);
+    const int64_t tiles = (n + corr::kRows - 1) / corr::kRows;
+    const unsigned grid = (unsigned)(tiles < 4 * (int64_t)h->num_sms ? tiles : 4 * (int64_t)h->num_sms);
+    const size_t sh = corr::kAlloc;
+    switch (k) {
+      case 0: k_advance32_mlp<0><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+      case 1: k_advance32_mlp<1><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+      case 2: k_advance32_mlp<2><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+      default: k_advance32_mlp<3><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+    }
+    PSTEP_LAUNCHED(h);
+  } else if (n > 0) {
     switch (k) {
       case 0: k_advance32<0><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word); break;
       case 1: k_advance32<1><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word); break;

@@ -13,8 +13,8 @@ from . import _lib
 
 FIELDS = ["RU_x", "RU_y", "RU_z", "Rho", "P", "T", "U_x", "U_y", "U_z", "C", "RHS_RU_x", "RHS_RU_y", "RHS_RU_z",
           "RHS_Part_Temp", "divergence", "Rho_new"]
-EXPORTS = ["pgas_create", "pgas_destroy", "pgas_set_stream", "pgas_init", "pgas_step", "pgas_get_field", "pgas_p0",
-           "pgas_last_iterations", "pgas_last_error"]
+EXPORTS = ["pgas_create", "pgas_destroy", "pgas_set_stream", "pgas_init", "pgas_step", "pgas_stage", "pgas_end_step",
+           "pgas_get_field", "pgas_p0", "pgas_last_iterations", "pgas_last_error"]
 
 _VP = C.c_void_p
 
@@ -36,6 +36,8 @@ def lib():
     L.pgas_set_stream.argtypes = [_VP, _VP]
     L.pgas_init.argtypes = [_VP, _VP] + [_VP] * 4 + [C.c_double, C.c_int]
     L.pgas_step.argtypes = [_VP, _VP]
+    L.pgas_stage.argtypes = [_VP, _VP, C.c_int]
+    L.pgas_end_step.argtypes = [_VP, _VP]
     L.pgas_get_field.argtypes = [_VP, C.c_int, _VP, C.c_int]
     L.pgas_p0.argtypes = [_VP, C.POINTER(C.c_double)]
     L.pgas_last_iterations.argtypes = [_VP]
@@ -93,6 +95,12 @@ class GasStep:
     def step(self, nsteps: int = 1):
         for _ in range(nsteps):
             self._ok(self.L.pgas_step(self.h, self._ph()))
+
+    def stage(self, k: int):
+        self._ok(self.L.pgas_stage(self.h, self._ph(), int(k)))
+
+    def end_step(self):
+        self._ok(self.L.pgas_end_step(self.h, self._ph()))
 
     def field(self, name: str) -> np.ndarray:
         g = self.n + 2

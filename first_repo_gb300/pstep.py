@@ -42,6 +42,11 @@ class Props(C.Structure):
                 ("alpha", C.c_void_p), ("accel", C.c_void_p * 3)]
 
 
+class Correction(C.Structure):
+    _fields_ = [("params", C.POINTER(C.c_float)), ("shift", C.c_float * 10), ("scale", C.c_float * 10),
+                ("lo", C.c_float * 4), ("hi", C.c_float * 4), ("prior_re", C.c_float), ("nu_gas", C.c_double)]
+
+
 class Config(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("bs", C.c_int32),
                 ("twc", C.c_int32), ("particle_gravity", C.c_int32), ("precision", C.c_int32),
@@ -56,7 +61,7 @@ _D = C.POINTER(C.c_double)
 _VP = C.c_void_p
 _H = C.c_void_p
 
-EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p", "pstep_set_particle_props",
+EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p", "pstep_set_particle_props", "pstep_set_correction",
            "pstep_num_particles", "pstep_bind_velocity", "pstep_bind_temperature", "pstep_prime",
            "pstep_stage_interp_advance_deposit", "pstep_wrap", "pstep_stage_temp", "pstep_stage",
            "pstep_end_stage", "pstep_end_step", "pstep_run", "pstep_get_field", "pstep_energy_mean",
@@ -76,6 +81,7 @@ def lib():
     L.pstep_upload_particles.argtypes = [_H, C.c_int64] + [_VP] * 8 + [C.c_int]
     L.pstep_set_tau_p.argtypes = [_H, _VP, C.c_int]
     L.pstep_set_particle_props.argtypes = [_H, C.POINTER(Props), C.c_int]
+    L.pstep_set_correction.argtypes = [_H, C.POINTER(Correction)]
     L.pstep_num_particles.argtypes = [_H]
     L.pstep_num_particles.restype = C.c_int64
     L.pstep_bind_velocity.argtypes = [_H, _VP, _VP, _VP, C.c_int]
@@ -206,6 +212,24 @@ class ParticleStep:
             for d in range(3):
                 pr.accel[d] = addr(accel[d])
         self._ok(self.L.pstep_set_particle_props(self.h, C.byref(pr), int(on_dev or 0)))
+
+    def set_correction(self, model, nu_gas: float | None = None):
+        """Learned correction (pstep_set_correction): model = dict(params, shift, scale, lo, hi)
+        as made by first_repo_gb300.learn, nu_gas the gas kinematic viscosity; None: off."""
+        if model is None:
+            self._ok(self.L.pstep_set_correction(self.h, None))
+            return
+        c = Correction()
+        self._corr_params = np.ascontiguousarray(model["params"], dtype=np.float32)
+        c.params = self._corr_params.ctypes.data_as(C.POINTER(C.c_float))
+        for name, n in (("shift", 10), ("scale", 10), ("lo", 4), ("hi", 4)):
+            vals = np.asarray(model[name], dtype=np.float64)
+            arr = getattr(c, name)
+            for i in range(n):
+                arr[i] = float(vals[i])
+        c.prior_re = float(model.get("prior_re", 0.0))
+        c.nu_gas = float(nu_gas if nu_gas is not None else model["nu_gas"])
+        self._ok(self.L.pstep_set_correction(self.h, C.byref(c)))
 
     @property
     def np(self) -> int:

@@ -150,6 +150,35 @@ typedef struct pstep_particle_props {
   const double *accel[3];    /* body acceleration, replaces ParticleGravity*g (particle.cpp:376-378) */
 } pstep_particle_props;
 int pstep_set_particle_props(pstep_handle h, const pstep_particle_props *props, int on_device);
+
+/* Learned correction of the interpolated gas state (FP32 form; no reference
+ * counterpart: the reference uses the disturbed interpolation, particle.cpp:340-360,
+ * 430-456). A network in the layout of pstep_mlp.h predicts, for every particle
+ * and stage, its own disturbance of the gas at x_int in units of the slip that
+ * drives it, y = d / |s| (learned where the drag used the disturbed slip s =
+ * u_int - u_plain). The step uses u_gas = u_plain - y[0..2] |s_drive| and
+ * Tg = Tg_plain - y[3] dT_drive, where s_drive and dT_drive are the slip and the
+ * T_new - Tg the particle's drag and heat transfer used in the previous stage
+ * (the plain values at the first stage; capped at 10x the plain ones): a fixed-
+ * point iteration across stages towards the self-consistent correction, which
+ * leaves the drag's dependence on the current gas value as in the plain step.
+ * The network runs on the tensor cores inside the advance kernel. Features,
+ * each mapped to (value - shift[i]) * scale[i]:
+ *   0-2 offset of x_int in its cell (cell units), 3-5 s_drive/|s_drive|, 6 d_p/dx,
+ *   7 ln Re_p with Re_p = |s_drive| d_p / nu_gas, 8 Q = alpha/(m_p Cvp), 9 ln tau_p;
+ * d_p is itth/(Nu*PI*k) with per-particle itth, else Dp. Particles with zero slip
+ * or with d_p/dx, Re_p, Q or tau_p outside [lo, hi] keep the plain values. */
+typedef struct pstep_correction {
+  const float *params;       /* PMLP_NPARAM floats, host memory */
+  float shift[10], scale[10];
+  float lo[4], hi[4];        /* ranges of d_p/dx, Re_p, Q, tau_p */
+  float prior_re;            /* > 0: the network's outputs are in units of the prior
+                                (d_p/dx) / (1 + Re_p / ((d_p/dx) prior_re)), the disturbance's
+                                dependence on size and cell Reynolds number; 0: no prior */
+  double nu_gas;             /* kinematic viscosity of the gas */
+} pstep_correction;
+/* NULL switches the correction off */
+int pstep_set_correction(pstep_handle h, const pstep_correction *c);
 int64_t pstep_num_particles(pstep_handle h);
 
 /* Gas fields, ghosted layout. The velocity is U = RU_int/Rho_face (grid.cpp:662),

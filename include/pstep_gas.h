@@ -55,8 +55,12 @@ int pgas_set_stream(pgas_handle g, void *cuda_stream);
  * uploaded, also the particle prime (pstep_prime) */
 int pgas_init(pgas_handle g, pstep_handle particles, const double *ru_x, const double *ru_y, const double *ru_z,
               const double *rho, double p0, int on_device);
-/* one time step of gas and particles */
+/* one time step of gas and particles: pgas_stage for k = 0..3, then pgas_end_step */
 int pgas_step(pgas_handle g, pstep_handle particles);
+/* RK4 stage k (simulation.cpp:40-48 and grid.cpp:705-712 for one k) */
+int pgas_stage(pgas_handle g, pstep_handle particles, int k);
+/* Correct_mean_RU and TimeAdvance (grid.cpp:566-572, 315-325) after stage 3 */
+int pgas_end_step(pgas_handle g, pstep_handle particles);
 int pgas_get_field(pgas_handle g, int id, double *dst, int on_device);
 /* thermodynamic pressure P0 after the last step */
 int pgas_p0(pgas_handle g, double *p0);
