@@ -1,7 +1,13 @@
 """Benchmark of the particle step: particle-steps/s on one GB300 (or N replicas).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload box512_clustered] [--form fp64|fp32]
+                    [--workload box512_corrected] [--form fp32mlp|fp32|fp64]
+
+The default line is the corrected step: the FP32 form with the learned
+correction fused into its advance (the committed network, BF16 tcgen05
+inference per particle and stage) on 512^3 cells x 2^27 particles with
+d_p/dx 0.5 and mass loading 1.0; the plain FP32 step and the FP64 drop-in run
+beside it on the same inputs (fp32_plain, fp64_dropin).
 
 A step is one RK4 step (4 stages + the per-step reorder) of every particle:
 interpolation, advance, wrap, and the concentration, momentum and energy
@@ -50,6 +56,10 @@ FP64_ADVANCE_CELL_BYTES = 4 * 8
 #   k=1..3 read base, *_int, *_np1 + RHS_T = 100 B; write 80 B.  fp32 fields U(3), T once per launch.
 FP32_ADVANCE_BYTES = {0: 36 + 80, 1: 100 + 80, 2: 100 + 80, 3: 100 + 80}
 FP32_ADVANCE_CELL_BYTES = 4 * 4
+# with the learned correction the advance also reads and writes the drive state
+# (slip 3 + temperature difference, fp32) of every particle: +32 B per particle and stage;
+# the network's weights (13 KB) are read once per CTA.
+FP32MLP_ADVANCE_EXTRA = 32
 # Deposits, per particle and per cell of one launch:
 #   FP32 (one fused walk): *_int cell+offsets (16) + RHS_u (12) + *_new cell+offsets (16) + RHS_T (4) = 48 B;
 #        per cell: cell_start (4) + five fp64 fields written (40) = 44 B.
@@ -60,6 +70,8 @@ FP32_ADVANCE_CELL_BYTES = 4 * 4
 PHASE_BYTES = {
     ("fp32", "advance"): (sum(FP32_ADVANCE_BYTES.values()) / 4.0, FP32_ADVANCE_CELL_BYTES),
     ("fp32", "deposit_int"): (48.0, 44.0),
+    ("fp32mlp", "advance"): (sum(FP32_ADVANCE_BYTES.values()) / 4.0 + FP32MLP_ADVANCE_EXTRA, FP32_ADVANCE_CELL_BYTES),
+    ("fp32mlp", "deposit_int"): (48.0, 44.0),
     ("fp64", "advance"): (sum(FP64_ADVANCE_BYTES.values()) / 4.0, FP64_ADVANCE_CELL_BYTES),
     ("fp64", "deposit_int"): (52.0, 36.0),
     ("fp64", "deposit_temp"): (36.0, 12.0),
@@ -136,10 +148,10 @@ def peaks():
         return FALLBACK_HBM, "fallback"
 
 
-def make_inputs(wl, dp_over_dx=0.1, mass_loading=0.2):
+def make_inputs(wl):
     t0 = time.time()
     case = gen.make_case(wl.n, wl.n_particles, wl.seed, wl.clustered)
-    bp = config.box_params(wl.n, wl.n_particles, dp_over_dx=dp_over_dx, mass_loading=mass_loading)
+    bp = config.box_params(wl.n, wl.n_particles, dp_over_dx=wl.dp_over_dx, mass_loading=wl.mass_loading)
     fields = [gen.ghost(case[k]) for k in ("ux", "uy", "uz", "T")]
     return case, bp, fields, time.time() - t0
 
@@ -221,9 +233,10 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="box512_clustered", choices=sorted(config.WORKLOADS))
-    ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--workload", default="box512_corrected", choices=sorted(config.WORKLOADS))
+    ap.add_argument("--form", default="fp32mlp", choices=["fp64", "fp32", "fp32mlp"])
     ap.add_argument("--no-fp64-line", action="store_true", help="skip timing the FP64 drop-in beside the FP32 form")
+    ap.add_argument("--no-fp32-line", action="store_true", help="skip timing the plain FP32 step beside fp32mlp")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -242,12 +255,30 @@ def main():
 
     from first_repo_gb300 import pstep
     case, bp, fields, gen_s = make_inputs(wl)
-    form = pstep.FP32 if args.form == "fp32" else pstep.FP64
+    form = pstep.FP64 if args.form == "fp64" else pstep.FP32
     flags = pstep.TRACK_ORDER if form == pstep.FP64 else 0
     n = wl.n_particles
     arrs = [np.ascontiguousarray(case[k]) for k in ("x", "y", "z", "u", "v", "w", "t", "flag")]
+    corr_model = None
+    if args.form == "fp32mlp":
+        from first_repo_gb300 import learn
+        corr_model = learn.load_model()
+    nu_gas = bp.mu0 / bp.rho0
+
+    def make_step(frm, flg, with_model):
+        h = pstep.ParticleStep(bp.step_config(), n, frm, flg)
+        h.load(*arrs)
+        if with_model:
+            h.set_correction(corr_model, nu_gas)
+        h.bind_velocity(*fields[:3])
+        h.bind_temperature(fields[3])
+        h.prime()
+        return h
+
     g = pstep.ParticleStep(bp.step_config(), n, form, flags)
     g.load(*arrs)
+    if corr_model is not None:
+        g.set_correction(corr_model, nu_gas)
     g.bind_velocity(*fields[:3])
     g.bind_temperature(fields[3])
     g.prime()
@@ -315,6 +346,8 @@ def main():
 
         def one_step():
             g.load(*hp)
+            if corr_model is not None:
+                g.set_correction(corr_model, nu_gas)
             g.bind_velocity(*hf[:3])
             g.bind_temperature(hf[3])
             g.prime()
@@ -338,22 +371,28 @@ def main():
                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3}
         del C
 
-    # the FP64 drop-in on the same inputs, timed the same way (the comparison the metric names)
+    # the plain FP32 step and the FP64 drop-in on the same inputs, timed the same way
+    # (the comparison the metric names)
+    fp32_plain = None
+    if args.form == "fp32mlp" and not args.no_fp32_line:
+        g.close()
+        g = make_step(pstep.FP32, 0, False)
+        for _ in range(args.warmup):
+            g.run(1)
+        barrier()
+        g.run(args.steps)
+        ms32 = g.last_run_ms() / args.steps
+        fp32_plain = {"value": world * n / (ms32 / 1e3), "ms_per_step": ms32, "form": "fp32 plain interpolation"}
     fp64 = None
     if form == pstep.FP32 and not args.no_fp64_line:
         g.close()
-        g64 = pstep.ParticleStep(bp.step_config(), n, pstep.FP64, pstep.TRACK_ORDER)
-        g64.load(*arrs)
-        g64.bind_velocity(*fields[:3])
-        g64.bind_temperature(fields[3])
-        g64.prime()
+        g = make_step(pstep.FP64, pstep.TRACK_ORDER, False)
         for _ in range(args.warmup):
-            g64.run(1)
+            g.run(1)
         barrier()
-        g64.run(args.steps)
-        ms64 = g64.last_run_ms() / args.steps
+        g.run(args.steps)
+        ms64 = g.last_run_ms() / args.steps
         fp64 = {"value": world * n / (ms64 / 1e3), "ms_per_step": ms64, "form": "fp64 drop-in (reference order)"}
-        g = g64
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -366,13 +405,17 @@ def main():
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == pstep.FP64 else "f32",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if form == pstep.FP64 else ("f32+bf16" if corr_model is not None else "f32"),
             "data": "synthetic",
             "config": {"workload": wl.name, "cells": wl.n ** 3, "particles": n, "form": args.form,
+                       "learned_correction": corr_model is not None, "dp_over_dx": wl.dp_over_dx,
+                       "mass_loading": wl.mass_loading,
                        "order_tracking": bool(flags & pstep.TRACK_ORDER), "clustered": wl.clustered,
                        "l2": "inputs larger than L2 (particle state alone is several GB)",
                        "parallelism": f"replicas x{world}", "input_generation_s": round(gen_s, 2)},
-            "roofline": roof, "phases": phases, "fp64_dropin": fp64, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roof, "phases": phases, "fp32_plain": fp32_plain, "fp64_dropin": fp64, "cpu_baseline": cpu,
+            "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }

@@ -118,6 +118,8 @@ class Workload:
     clustered: bool
     steps: int
     seed: int
+    dp_over_dx: float = 0.1
+    mass_loading: float = 0.2
 
 
 # Seeded synthetic stand-ins for the reference's run shapes.
@@ -125,6 +127,8 @@ WORKLOADS = {
     "box64_uniform": Workload("box64_uniform", 64, 1 << 15, False, 1, 1001),
     "box256_clustered": Workload("box256_clustered", 256, 1 << 24, True, 10, 1002),
     "box512_clustered": Workload("box512_clustered", 512, 1 << 27, True, 1, 1003),
+    # the corrected-step workload: larger, heavier particles (d_p/dx 0.5, mass loading 1.0)
+    "box512_corrected": Workload("box512_corrected", 512, 1 << 27, True, 100, 1004, 0.5, 1.0),
 }
 
 
