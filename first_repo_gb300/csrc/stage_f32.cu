@@ -84,6 +84,8 @@ struct F32Form {
   float *pp[7];    // per-particle mass ratio, itth, 1/(m Cvp), alpha, body acceleration x y z (or nullptr)
   float *gas[4];   // ug vg wg at x_int and Tg - t_ref at x_new of the last stage (PSTEP_KEEP_GAS)
   float *drive[4]; // learned correction: the slip (3) and T_new - Tg the last stage's drag and heat transfer used
+  uint2 *corr_y;   // learned correction: the network output of the step's stage 0 (bf16 x 4)
+  uint2 *corr_y_tmp;  // its permutation scratch
   float *rhs_u[3];
   float *uf[3], *tf;  // fp32 ghosted copies of the bound fields
   uint32_t *key;      // brick-major cell id of the base position
@@ -178,18 +180,33 @@ struct Adv {
   float gas[3];
 };
 
+// the particle's x_int cell, offsets and velocity and the gas velocity there (particle.cpp:340-360)
 template <int K>
-__device__ __forceinline__ void adv_load(const Geom &G, const F32Form &f, const C32 &c, int64_t p, Adv &a) {
+__device__ __forceinline__ void adv_load_gas(const Geom &G, const F32Form &f, int64_t p, Adv &a) {
+  const Set32 &I = (K == 0) ? f.set[SBASE] : f.set[SINT];
+  a.cint = I.cell[p];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) { a.oin[d] = I.o[d][p]; a.vin[d] = I.v[d][p]; }
+  const int ii = ci_(a.cint) + 1, jj = cj_(a.cint) + 1, kk = ck_(a.cint) + 1;
+  const float xl = a.oin[0], yl = a.oin[1], zl = a.oin[2];
+  a.gas[0] = xl * f.uf[0][glin3(G, ii + 1, jj, kk)] + (1.f - xl) * f.uf[0][glin3(G, ii, jj, kk)];
+  a.gas[1] = yl * f.uf[1][glin3(G, ii, jj + 1, kk)] + (1.f - yl) * f.uf[1][glin3(G, ii, jj, kk)];
+  a.gas[2] = zl * f.uf[2][glin3(G, ii, jj, kk + 1)] + (1.f - zl) * f.uf[2][glin3(G, ii, jj, kk)];
+}
+
+// everything else the stage reads
+template <int K>
+__device__ __forceinline__ void adv_load_rest(const Geom &G, const F32Form &f, const C32 &c, int64_t p, Adv &a) {
   const Set32 &B = f.set[SBASE];
   const Set32 &I = (K == 0) ? f.set[SBASE] : f.set[SINT];
   const Set32 &A = (K == 0) ? f.set[SBASE] : f.set[SNP1];
   a.cb = B.cell[p];
-  a.cint = I.cell[p];
   a.cacc = A.cell[p];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) { a.ob[d] = B.o[d][p]; a.oin[d] = I.o[d][p]; a.oac[d] = A.o[d][p]; }
+  for (int d = 0; d < 3; ++d) { a.ob[d] = B.o[d][p]; a.oac[d] = A.o[d][p]; }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) { a.vb[q] = B.v[q][p]; a.vin[q] = I.v[q][p]; a.vac[q] = A.v[q][p]; }
+  for (int q = 0; q < 4; ++q) { a.vb[q] = B.v[q][p]; a.vac[q] = A.v[q][p]; }
+  a.vin[3] = I.v[3][p];
   a.rhs_t_old = f.rhs_t[p];
   a.itp = f.itp ? f.itp[p] : c.itp;
   a.itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
@@ -198,12 +215,12 @@ __device__ __forceinline__ void adv_load(const Geom &G, const F32Form &f, const 
   a.dpost_is = f.pp[PP_HEAT_IS] ? c.dt_post * f.pp[PP_HEAT_IS][p] : c.dt_post_is;
 #pragma unroll
   for (int d = 0; d < 3; ++d) a.gacc[d] = f.pp[PP_ACC + d] ? f.pp[PP_ACC + d][p] : c.g[d];
-  // face-normal interpolation at x_int (particle.cpp:340-360)
-  const int ii = ci_(a.cint) + 1, jj = cj_(a.cint) + 1, kk = ck_(a.cint) + 1;
-  const float xl = a.oin[0], yl = a.oin[1], zl = a.oin[2];
-  a.gas[0] = xl * f.uf[0][glin3(G, ii + 1, jj, kk)] + (1.f - xl) * f.uf[0][glin3(G, ii, jj, kk)];
-  a.gas[1] = yl * f.uf[1][glin3(G, ii, jj + 1, kk)] + (1.f - yl) * f.uf[1][glin3(G, ii, jj, kk)];
-  a.gas[2] = zl * f.uf[2][glin3(G, ii, jj, kk + 1)] + (1.f - zl) * f.uf[2][glin3(G, ii, jj, kk)];
+}
+
+template <int K>
+__device__ __forceinline__ void adv_load(const Geom &G, const F32Form &f, const C32 &c, int64_t p, Adv &a) {
+  adv_load_gas<K>(G, f, p, a);
+  adv_load_rest<K>(G, f, c, p, a);
 }
 
 // The rest of the stage for one particle, with a.gas the gas velocity to use; with
@@ -324,22 +341,33 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
 // ----------------------------------------------------------------------------
 // The learned correction fused into the advance (pstep_set_correction).
 //
-// Persistent CTAs of 128 threads, one particle per thread and tile of 128
-// particles; thread t's network row is tensor-memory lane t. Per tile: plain
-// interpolation and features in registers, the feature row as bf16 to shared
-// memory, three tcgen05 MMAs (16 -> 64 -> 64 -> 16 columns, accumulators in
-// tensor memory, bias and SiLU between them in registers), then the corrected
-// gas velocity and temperature feed the same finish as the plain step.
+// Stage 0 runs the network: persistent CTAs of two warpgroups; each warpgroup
+// owns tiles of 128 particles, one particle per thread, and thread t's network
+// row is tensor-memory lane t of the warpgroup's 64 columns. Per tile: the plain
+// interpolation and the features in registers, the feature row as bf16 to shared
+// memory, three tcgen05 MMAs (16 -> 64 -> 64 -> 16 columns; each layer's
+// accumulator reuses the columns of the one before, which has been read), bias
+// and SiLU between them on 16-column chunks, then the corrected gas values feed
+// the same finish as the plain step. The two warpgroups synchronise with named
+// barriers only, so one's MMAs overlap the other's loads and epilogues. The
+// network output (bf16 x 4) is kept per particle for stages 1-3, which apply it
+// with their own drive slip and prior: within a step a particle moves less than
+// a few hundredths of a cell and its slip hardly changes.
 // Particles outside the training ranges keep the plain interpolation.
 namespace corr {
-constexpr int kRows = 128, kInP = 16, kHid = 64, kOutP = 16;
-constexpr uint32_t W1 = 0, W2 = W1 + kHid * kInP * 2, W3 = W2 + kHid * kHid * 2, XA = W3 + kOutP * kHid * 2,
-                   H1A = XA + kRows * kInP * 2, H2A = H1A + kRows * kHid * 2, BIAS = H2A + kRows * kHid * 2,
-                   MISC = BIAS + (kHid + kHid + kOutP) * 4, kBytes = MISC + 64;
-constexpr uint32_t kImage = XA;  // packed weight image: W1 | W2 | W3 tiles, bf16
-// at most 4 CTAs fit on an SM, so 4 x 128 tensor-memory columns never exceed 512
-constexpr uint32_t kAlloc = 52 * 1024;
-static_assert(kBytes <= kAlloc, "correction smem");
+constexpr int kRows = 128, kInP = 16, kHid = 64, kOutP = 16, kGroups = 2, kThreads = kRows * kGroups;
+// shared memory: weight image W1 | W2 | W3 (bf16 tiles), biases, then per warpgroup
+// X [128 x 16], H [128 x 64] (layer 1, then layer 2 output) and its mbarrier
+constexpr uint32_t W1 = 0, W2 = W1 + kHid * kInP * 2, W3 = W2 + kHid * kHid * 2, kImage = W3 + kOutP * kHid * 2;
+constexpr uint32_t BIAS = kImage, GROUPS = 13 * 1024;
+constexpr uint32_t G_XA = 0, G_H = G_XA + kRows * kInP * 2, G_BAR = G_H + kRows * kHid * 2, kGroupStride = 21 * 1024;
+constexpr uint32_t TSLOT = GROUPS + kGroups * kGroupStride, kBytes = TSLOT + 16;
+static_assert(BIAS + (kHid + kHid + kOutP) * 4 <= GROUPS, "correction smem");
+static_assert(G_BAR + 8 <= kGroupStride, "correction group smem");
+// with this much shared memory at most 4 CTAs fit on an SM (228 KB), so their
+// 4 x 128 tensor-memory columns never exceed the 512 an SM has and no allocation waits
+constexpr uint32_t kAlloc = kBytes;
+static_assert(5 * (kAlloc + 1024) > 228 * 1024, "more than 4 correction CTAs per SM");
 constexpr uint32_t kWaitLimit = 1u << 22;
 }  // namespace corr
 
@@ -361,189 +389,268 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   return *reinterpret_cast<uint32_t *>(&v);
 }
 
-template <int C>
-__device__ __forceinline__ void corr_row(uint8_t *tile, int r, const float *v) {
-#pragma unroll
-  for (int cb = 0; cb < C / 8; ++cb) {
-    uint4 q;
-    q.x = pack_bf16x2(v[cb * 8 + 0], v[cb * 8 + 1]);
-    q.y = pack_bf16x2(v[cb * 8 + 2], v[cb * 8 + 3]);
-    q.z = pack_bf16x2(v[cb * 8 + 4], v[cb * 8 + 5]);
-    q.w = pack_bf16x2(v[cb * 8 + 6], v[cb * 8 + 7]);
-    *reinterpret_cast<uint4 *>(tile + tc05::tile_off(r, cb * 8, C)) = q;
-  }
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
+// SiLU z * sigmoid(z) = z/2 * (1 + tanh(z/2)) with the hardware tanh approximation
+__device__ __forceinline__ float silu_fast(float z) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+  return 0.5f * z * (1.f + t);
 }
 
-__device__ __forceinline__ void corr_sync() {
+// warpgroup-local barrier (named barrier 1 + group, 128 threads; immediate ids)
+__device__ __forceinline__ void group_bar(int wg) {
+  if (wg == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+  else asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+__device__ __forceinline__ bool group_and(int wg, bool v) {
+  uint32_t out;
+  if (wg == 0)
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, 1, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(out)
+        : "r"(v ? 1u : 0u)
+        : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, 2, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(out)
+        : "r"(v ? 1u : 0u)
+        : "memory");
+  return out != 0;
+}
+__device__ __forceinline__ void group_sync_mma(int wg) {
   tc05::fence_smem_async();
   tc05::fence_before();
-  __syncthreads();
+  group_bar(wg);
   tc05::fence_after();
 }
-
-__device__ __forceinline__ bool corr_wait(uint64_t *mbar, uint32_t &phase) {
+__device__ __forceinline__ bool group_wait(int wg, uint64_t *mbar, uint32_t &phase) {
   const bool ok = tc05::mbar_wait(mbar, phase, corr::kWaitLimit);
   tc05::fence_after();
-  const bool all = __syncthreads_and(ok ? 1 : 0) != 0;
+  const bool all = group_and(wg, ok);
   if (all) phase ^= 1u;
   return all;
 }
 
+// 16 accumulator columns + bias -> SiLU -> bf16, into row r, columns [c0, c0+16) of a 64-column tile
+__device__ __forceinline__ void silu_chunk_to_tile(uint8_t *tile, int r, int c0, const float (&v)[16],
+                                                   const float *bias) {
+  float h[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) h[q] = silu_fast(v[q] + bias[c0 + q]);
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    uint4 w;
+    w.x = pack_bf16x2(h[half * 8 + 0], h[half * 8 + 1]);
+    w.y = pack_bf16x2(h[half * 8 + 2], h[half * 8 + 3]);
+    w.z = pack_bf16x2(h[half * 8 + 4], h[half * 8 + 5]);
+    w.w = pack_bf16x2(h[half * 8 + 6], h[half * 8 + 7]);
+    *reinterpret_cast<uint4 *>(tile + tc05::tile_off(r, c0 + half * 8, corr::kHid)) = w;
+  }
+}
+
+// the drive slip: the previous stage's (at most kDriveCap x the plain one), or the plain slip
+__device__ __forceinline__ void drive_slip(const F32Form &f, int64_t p, const float (&s)[3], float smag, float &sdrv,
+                                           float (&dir)[3], float &dmag_used) {
+  const float d0 = f.drive[0][p], d1 = f.drive[1][p], d2 = f.drive[2][p];
+  const float dmag = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+  if (dmag > 0.f) {
+    sdrv = fminf(dmag, kDriveCap * smag);
+    dir[0] = d0; dir[1] = d1; dir[2] = d2;
+    dmag_used = dmag;
+  } else {
+    sdrv = smag;
+    dir[0] = s[0]; dir[1] = s[1]; dir[2] = s[2];
+    dmag_used = smag;
+  }
+}
+
+__device__ __forceinline__ float prior_of(const CorrDev &cd, float dpdx, float rep) {
+  return cd.inv_prior_re > 0.f ? dpdx / (1.f + rep / dpdx * cd.inv_prior_re) : 1.f;
+}
+
+__device__ __forceinline__ float particle_dp(const F32Form &f, const CorrDev &cd, int64_t p, float itth) {
+  return f.pp[PP_ITTH] ? itth * cd.dp_per_itth : cd.dp;
+}
+
 template <int K>
-__global__ void __launch_bounds__(128, 4) k_advance32_mlp(Geom G, F32Form f, C32 c, int twc, int64_t n,
-                                                          int32_t *__restrict__ err, CorrDev cd) {
+__global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32Form f, C32 c, int twc, int64_t n,
+                                                                     int32_t *__restrict__ err, CorrDev cd) {
   extern __shared__ __align__(1024) uint8_t sm[];
   using namespace tc05;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  uint8_t *W1 = sm + corr::W1, *W2 = sm + corr::W2, *W3 = sm + corr::W3, *XA = sm + corr::XA, *H1A = sm + corr::H1A,
-          *H2A = sm + corr::H2A;
+  const int tid = threadIdx.x, wg = tid >> 7, lt = tid & (corr::kRows - 1), warp = tid >> 5;
+  uint8_t *W1 = sm + corr::W1, *W2 = sm + corr::W2, *W3 = sm + corr::W3;
   float *b1 = reinterpret_cast<float *>(sm + corr::BIAS), *b2 = b1 + corr::kHid, *b3 = b2 + corr::kHid;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + corr::MISC);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + corr::MISC + 8);
-  for (uint32_t q = tid; q < corr::kImage / 16; q += corr::kRows) reinterpret_cast<uint4 *>(sm)[q] = cd.image[q];
-  for (int q = tid; q < corr::kHid + corr::kHid + corr::kOutP; q += corr::kRows) b1[q] = cd.bias[q];
-  if (tid == 0) mbar_init(mbar, 1);
+  uint8_t *gbase = sm + corr::GROUPS + wg * corr::kGroupStride;
+  uint8_t *XA = gbase + corr::G_XA, *H = gbase + corr::G_H;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(gbase + corr::G_BAR);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + corr::TSLOT);
+  for (uint32_t q = tid; q < corr::kImage / 16; q += corr::kThreads) reinterpret_cast<uint4 *>(sm)[q] = cd.image[q];
+  for (int q = tid; q < corr::kHid + corr::kHid + corr::kOutP; q += corr::kThreads) b1[q] = cd.bias[q];
+  if (lt == 0) mbar_init(mbar, 1);
   if (warp == 0) tmem_alloc(tslot, 128);
-  corr_sync();
-  const uint32_t tm = *tslot;
-  const uint32_t tl = tm + ((uint32_t)(warp * 32) << 16);
+  tc05::fence_smem_async();
+  tc05::fence_before();
+  __syncthreads();
+  tc05::fence_after();
+  const uint32_t tcol = *tslot + (uint32_t)(wg * 64);
+  const uint32_t tl = tcol + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lane quadrant
   const uint32_t id64 = idesc_bf16(128, 64), id16 = idesc_bf16(128, 16);
+  const uint32_t sX = smem_u32(XA), sH = smem_u32(H), sW1 = smem_u32(W1), sW2 = smem_u32(W2), sW3 = smem_u32(W3);
   uint32_t phase = 0;
   bool ok = true;
   float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
   const int64_t ntiles = (n + corr::kRows - 1) / corr::kRows;
-  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    const int64_t p = tile * corr::kRows + tid;
+  for (int64_t tile = (int64_t)blockIdx.x * corr::kGroups + wg; tile < ntiles && ok;
+       tile += (int64_t)gridDim.x * corr::kGroups) {
+    const int64_t p = tile * corr::kRows + lt;
     const bool live = p < n;
+    // phase A: the plain interpolation and the features; only these stay live across the MMAs
     Adv a;
-    float x[corr::kInP];
-#pragma unroll
-    for (int j = 0; j < corr::kInP; ++j) x[j] = 0.f;
-    float smag = 0.f, sdrv = 0.f, prior = 1.f;
+    float sdrv = 0.f, prior = 1.f, smag = 0.f;
     bool use = false;
-    if (live) {
-      adv_load<K>(G, f, c, p, a);
-      // features (pstep.h, pstep_correction) from the slip that drives the drag: the previous
-      // stage's (at most kDriveCap x the plain slip), or the plain slip when there is none
-      float s0 = a.vin[0] - a.gas[0], s1 = a.vin[1] - a.gas[1], s2 = a.vin[2] - a.gas[2];
-      smag = sqrtf(s0 * s0 + s1 * s1 + s2 * s2);
-      const float d0 = f.drive[0][p], d1 = f.drive[1][p], d2 = f.drive[2][p];
-      const float dmag = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-      sdrv = smag;
-      if (dmag > 0.f) {
-        sdrv = fminf(dmag, kDriveCap * smag);
-        s0 = d0;
-        s1 = d1;
-        s2 = d2;
-      }
-      const float smagd = dmag > 0.f ? dmag : smag;
-      const float dp = f.pp[PP_ITTH] ? a.itth * cd.dp_per_itth : cd.dp;
-      const float dpdx = dp * cd.idx;
-      const float rep = sdrv * dp * cd.inv_nu;
-      const float his = f.pp[PP_HEAT_IS] ? f.pp[PP_HEAT_IS][p] : c.is;
-      const float q = a.alpha * his;
-      const float taup = 1.f / a.itp;
-      if (cd.inv_prior_re > 0.f) prior = dpdx / (1.f + rep / dpdx * cd.inv_prior_re);
-      use = smag > 0.f && smagd > 0.f && dpdx >= cd.lo[0] && dpdx <= cd.hi[0] && rep >= cd.lo[1] && rep <= cd.hi[1] &&
-            q >= cd.lo[2] && q <= cd.hi[2] && taup >= cd.lo[3] && taup <= cd.hi[3];
-      if (use) {
-        const float inv = 1.f / smagd;
-        const float raw[10] = {a.oin[0], a.oin[1], a.oin[2], s0 * inv, s1 * inv, s2 * inv, dpdx, logf(rep), q,
-                               logf(taup)};
-#pragma unroll
-        for (int j = 0; j < 10; ++j) x[j] = (raw[j] - cd.shift[j]) * cd.scale[j];
-      }
-    }
-    corr_row<corr::kInP>(XA, tid, x);
-    corr_sync();
-    if (tid == 0) {
-      mma_bf16(tm, tile_desc(smem_u32(XA), corr::kInP, 0, 0), tile_desc(smem_u32(W1), corr::kInP, 0, 0), id64, 0);
-      commit(mbar);
-    }
-    ok = corr_wait(mbar, phase);
-    if (!ok) break;
     {
-      float h[corr::kHid];
+      float x[corr::kInP];
 #pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
-        float v[16];
-        tmem_ld16(tl + cc * 16, v);
+      for (int j = 0; j < corr::kInP; ++j) x[j] = 0.f;
+      if (live) {
+        adv_load_gas<K>(G, f, p, a);
+        const float s[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
+        smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+        float dir[3], dmag;
+        drive_slip(f, p, s, smag, sdrv, dir, dmag);
+        const float itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
+        const float itp = f.itp ? f.itp[p] : c.itp;
+        const float alpha = f.pp[PP_ALPHA] ? f.pp[PP_ALPHA][p] : c.alpha;
+        const float his = f.pp[PP_HEAT_IS] ? f.pp[PP_HEAT_IS][p] : c.is;
+        const float dpdx = particle_dp(f, cd, p, itth) * cd.idx;
+        const float rep = sdrv * particle_dp(f, cd, p, itth) * cd.inv_nu;
+        const float q = alpha * his;
+        const float taup = 1.f / itp;
+        prior = prior_of(cd, dpdx, rep);
+        use = smag > 0.f && dmag > 0.f && dpdx >= cd.lo[0] && dpdx <= cd.hi[0] && rep >= cd.lo[1] &&
+              rep <= cd.hi[1] && q >= cd.lo[2] && q <= cd.hi[2] && taup >= cd.lo[3] && taup <= cd.hi[3];
+        if (use) {
+          const float inv = 1.f / dmag;
+          const float raw[10] = {a.oin[0], a.oin[1], a.oin[2], dir[0] * inv, dir[1] * inv, dir[2] * inv, dpdx,
+                                 logf(rep), q, logf(taup)};
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const float z = v[q] + b1[cc * 16 + q];
-          h[cc * 16 + q] = z / (1.f + expf(-z));
+          for (int j = 0; j < 10; ++j) x[j] = (raw[j] - cd.shift[j]) * cd.scale[j];
         }
       }
-      corr_row<corr::kHid>(H1A, tid, h);
-    }
-    corr_sync();
-    if (tid == 0) {
 #pragma unroll
-      for (int ks = 0; ks < 4; ++ks)
-        mma_bf16(tm + 64, tile_desc(smem_u32(H1A), corr::kHid, 0, ks), tile_desc(smem_u32(W2), corr::kHid, 0, ks), id64, ks);
-      commit(mbar);
-    }
-    ok = corr_wait(mbar, phase);
-    if (!ok) break;
-    {
-      float h[corr::kHid];
-#pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
-        float v[16];
-        tmem_ld16(tl + 64 + cc * 16, v);
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const float z = v[q] + b2[cc * 16 + q];
-          h[cc * 16 + q] = z / (1.f + expf(-z));
-        }
+      for (int cb = 0; cb < 2; ++cb) {
+        uint4 w;
+        w.x = pack_bf16x2(x[cb * 8 + 0], x[cb * 8 + 1]);
+        w.y = pack_bf16x2(x[cb * 8 + 2], x[cb * 8 + 3]);
+        w.z = pack_bf16x2(x[cb * 8 + 4], x[cb * 8 + 5]);
+        w.w = pack_bf16x2(x[cb * 8 + 6], x[cb * 8 + 7]);
+        *reinterpret_cast<uint4 *>(XA + tile_off(lt, cb * 8, corr::kInP)) = w;
       }
-      corr_row<corr::kHid>(H2A, tid, h);
     }
-    corr_sync();
-    if (tid == 0) {  // D3 reuses columns [0, 16): D1 has been read
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks)
-        mma_bf16(tm, tile_desc(smem_u32(H2A), corr::kHid, 0, ks), tile_desc(smem_u32(W3), corr::kHid, 0, ks), id16, ks);
+    group_sync_mma(wg);
+    if (lt == 0) {
+      mma_bf16(tcol, tile_desc(sX, corr::kInP, 0, 0), tile_desc(sW1, corr::kInP, 0, 0), id64, 0);
       commit(mbar);
     }
-    ok = corr_wait(mbar, phase);
+    ok = group_wait(wg, mbar, phase);
+    if (!ok) break;
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+      float v[16];
+      tmem_ld16(tl + cc * 16, v);
+      silu_chunk_to_tile(H, lt, cc * 16, v, b1);
+    }
+    group_sync_mma(wg);
+    if (lt == 0) {  // layer 2 into the same columns (layer 1 has been read)
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks)
+        mma_bf16(tcol, tile_desc(sH, corr::kHid, 0, ks), tile_desc(sW2, corr::kHid, 0, ks), id64, ks);
+      commit(mbar);
+    }
+    ok = group_wait(wg, mbar, phase);
+    if (!ok) break;
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {  // layer 2 output overwrites layer 1's in H (its MMA is done)
+      float v[16];
+      tmem_ld16(tl + cc * 16, v);
+      silu_chunk_to_tile(H, lt, cc * 16, v, b2);
+    }
+    group_sync_mma(wg);
+    if (lt == 0) {
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks)
+        mma_bf16(tcol, tile_desc(sH, corr::kHid, 0, ks), tile_desc(sW3, corr::kHid, 0, ks), id16, ks);
+      commit(mbar);
+    }
+    ok = group_wait(wg, mbar, phase);
     if (!ok) break;
     float y[16];
     tmem_ld16(tl, y);
+    tc05::fence_before();  // the accumulator reads before the warpgroup's next MMA
     if (live) {
-      // The network gives the disturbance per unit of the slip (excess temperature) that drove
-      // it, y = d/|s|, learned where the drag used the disturbed slip. Here the drag uses the
-      // corrected slip, so the disturbance is scaled by the slip (temperature difference) the
-      // particle's drag (heat transfer) used in the previous stage: a fixed-point iteration
-      // across stages towards d = y |s_drive|, s_drive = s + d, that leaves the drag's
-      // dependence on the current gas value as in the plain step. The drive is capped at
-      // kDriveCap x the plain value (self-consistent up to k = y . s/|s| = 1 - 1/kDriveCap).
-      float ty = 0.f, tdrive = 0.f;
-      const float td_prev = f.drive[3][p];
+      // phase B: the rest of the particle, the correction, the finish
+      adv_load_rest<K>(G, f, c, p, a);
+      float yo[4] = {0.f, 0.f, 0.f, 0.f};
+      float ty = 0.f;
       if (use) {
-        const float y0 = (y[0] + b3[0]) * prior, y1 = (y[1] + b3[1]) * prior, y2 = (y[2] + b3[2]) * prior;
-        a.gas[0] -= sdrv * y0;
-        a.gas[1] -= sdrv * y1;
-        a.gas[2] -= sdrv * y2;
-        ty = (y[3] + b3[3]) * prior;
-        tdrive = td_prev;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) yo[d] = y[d] + b3[d];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) a.gas[d] -= sdrv * prior * yo[d];
+        ty = prior * yo[3];
       }
+      f.corr_y[p] = make_uint2(pack_bf16x2(yo[0], yo[1]), pack_bf16x2(yo[2], yo[3]));
       f.drive[0][p] = a.vin[0] - a.gas[0];
       f.drive[1][p] = a.vin[1] - a.gas[1];
       f.drive[2][p] = a.vin[2] - a.gas[2];
-      f.drive[3][p] = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, tdrive, err, mu0, mu1, mu2, mt);
+      f.drive[3][p] = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, use ? f.drive[3][p] : 0.f, err, mu0, mu1, mu2, mt);
     }
-    tc05::fence_before();  // this tile's tensor-memory reads before the next tile's MMAs
   }
   if (!ok) {
-    if (tid == 0) atomicOr(err, kErrTimeout);
+    if (lt == 0) atomicOr(err, kErrTimeout);
     tc05::mbar_wait(mbar, phase, corr::kWaitLimit);
   }
   block_max4(f.slots, mu0, mu1, mu2, mt);
   tc05::fence_before();
   __syncthreads();
   tc05::fence_after();
-  if (warp == 0) tmem_dealloc(tm, 128);
+  if (warp == 0) tmem_dealloc(*tslot, 128);
+}
+
+// stages 1-3 with the correction: the network output of the step's stage 0, applied with
+// this stage's drive slip and prior
+template <int K>
+__global__ void __launch_bounds__(256) k_advance32_corr(Geom G, F32Form f, C32 c, int twc, int64_t n,
+                                                        int32_t *__restrict__ err, CorrDev cd) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
+  if (p < n) {
+    Adv a;
+    adv_load<K>(G, f, c, p, a);
+    const uint2 yw = f.corr_y[p];
+    const float yo[4] = {bf16_lo(yw.x), bf16_hi(yw.x), bf16_lo(yw.y), bf16_hi(yw.y)};
+    float ty = 0.f, td = 0.f;
+    if (yo[0] != 0.f || yo[1] != 0.f || yo[2] != 0.f || yo[3] != 0.f) {
+      const float s[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
+      const float smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+      float sdrv, dir[3], dmag;
+      drive_slip(f, p, s, smag, sdrv, dir, dmag);
+      const float dp = particle_dp(f, cd, p, a.itth);
+      const float prior = prior_of(cd, dp * cd.idx, sdrv * dp * cd.inv_nu);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) a.gas[d] -= sdrv * prior * yo[d];
+      ty = prior * yo[3];
+      td = f.drive[3][p];
+    }
+    f.drive[0][p] = a.vin[0] - a.gas[0];
+    f.drive[1][p] = a.vin[1] - a.gas[1];
+    f.drive[2][p] = a.vin[2] - a.gas[2];
+    f.drive[3][p] = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, td, err, mu0, mu1, mu2, mt);
+  }
+  block_max4(f.slots, mu0, mu1, mu2, mt);
 }
 
 // the prime (grid.cpp:223-226) at the base positions: Tg, RHS_T
@@ -1079,6 +1186,11 @@ int sort_step(pstep_ctx *h) {
       if (f.gas[q]) permf(f.gas[q]);
     for (int q = 0; q < 4; ++q)
       if (f.drive[q]) permf(f.drive[q]);
+    if (f.corr_y) {
+      k_perm<uint2><<<nb(n), kThreads, 0, h->stream>>>(f.corr_y, f.sidx, n, f.corr_y_tmp);
+      uint2 *t = f.corr_y; f.corr_y = f.corr_y_tmp; f.corr_y_tmp = t;
+      h->launches += 1;
+    }
     {
       k_perm<uint32_t><<<nb(n), kThreads, 0, h->stream>>>(B.cell, f.sidx, n, (uint32_t *)f.tmpf);
       uint32_t *t = B.cell; B.cell = (uint32_t *)f.tmpf; f.tmpf = (float *)t;
@@ -1182,6 +1294,7 @@ int f32_destroy(pstep_ctx *h) {
   for (int q = 0; q < 7; ++q) dfree32(f->pp[q]);
   for (int q = 0; q < 4; ++q) dfree32(f->gas[q]);
   for (int q = 0; q < 4; ++q) dfree32(f->drive[q]);
+  dfree32(f->corr_y); dfree32(f->corr_y_tmp);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx); dfree32(f->tmpf);
   dfree32(f->bounds); dfree32(f->se); dfree32(f->slots);
@@ -1204,6 +1317,7 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
   for (int q = 0; q < 7; ++q) dfree32(f.pp[q]);
   for (int q = 0; q < 4; ++q)
     if (f.drive[q]) PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
+  if (f.corr_y) PSTEP_CUDA(cudaMemsetAsync(f.corr_y, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   f.sorted = 0;
   if (n == 0) return PSTEP_OK;
   if (!f.tref_set) {
@@ -1366,9 +1480,6 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_advance32_mlp<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
-    cudaFuncSetAttribute(k_advance32_mlp<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
-    cudaFuncSetAttribute(k_advance32_mlp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
-    cudaFuncSetAttribute(k_advance32_mlp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
     PSTEP_CUDA(cudaGetLastError());
     attr = true;
   }
@@ -1376,6 +1487,9 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
     if (!f.drive[q]) TRY32(dalloc32(h, f.drive[q], (size_t)h->cap));
     PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
   }
+  if (!f.corr_y) TRY32(dalloc32(h, f.corr_y, (size_t)h->cap));
+  if (!f.corr_y_tmp) TRY32(dalloc32(h, f.corr_y_tmp, (size_t)h->cap));
+  PSTEP_CUDA(cudaMemsetAsync(f.corr_y, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   h->corr_on = 1;
   return PSTEP_OK;
 }
@@ -1418,16 +1532,19 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
   const int64_t n = h->np;
   prof_begin(h, PSTEP_PHASE_ADVANCE);
   if (n > 0 && h->corr_on) {
-    // persistent: 4 CTAs per SM (the tensor-memory and shared-memory budget), tiles of 128 particles
     const CorrDev &cd = *reinterpret_cast<const CorrDev *>(h->corr_dev);
-    const int64_t tiles = (n + corr::kRows - 1) / corr::kRows;
-    const unsigned grid = (unsigned)(tiles < 4 * (int64_t)h->num_sms ? tiles : 4 * (int64_t)h->num_sms);
-    const size_t sh = corr::kAlloc;
-    switch (k) {
-      case 0: k_advance32_mlp<0><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
-      case 1: k_advance32_mlp<1><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
-      case 2: k_advance32_mlp<2><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
-      default: k_advance32_mlp<3><<<grid, corr::kRows, sh, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+    if (k == 0) {
+      // the network: persistent CTAs of two warpgroups, 3 per SM, tiles of 128 particles
+      const int64_t pairs = (n + 2 * corr::kRows - 1) / (2 * corr::kRows);
+      const unsigned grid = (unsigned)(pairs < 3 * (int64_t)h->num_sms ? pairs : 3 * (int64_t)h->num_sms);
+      k_advance32_mlp<0><<<grid, corr::kThreads, corr::kAlloc, h->stream>>>(h->geom, f, c, h->cfg.twc, n,
+                                                                            h->err_word, cd);
+    } else if (k == 1) {
+      k_advance32_corr<1><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd);
+    } else if (k == 2) {
+      k_advance32_corr<2><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd);
+    } else {
+      k_advance32_corr<3><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd);
     }
     PSTEP_LAUNCHED(h);
   } else if (n > 0) {
