@@ -44,10 +44,8 @@ int fold_fields(pstep_ctx *h, double *const *f, int nf, int refresh);
 namespace pstep {
 
 enum { SBASE = 0, SINT = 1, SNEW = 2, SNP1 = 3 };
-constexpr int kBr = 8;            // brick edge (cells) for the sort order and the deposit CTAs
-constexpr int kHalo = 2;          // source cells beyond the brick
-constexpr int kSrc = kBr + 2 * kHalo;
-constexpr int kDepThreads = 256;
+constexpr int kBr = 8;            // brick edge (cells) of the sort order
+constexpr int kHalo = 2;          // source cells beyond a deposit brick
 constexpr int kMaxN = 1024;       // 10 bits per cell coordinate
 constexpr int kBoundSlots = 1024;
 
@@ -57,12 +55,23 @@ struct Set32 {
   float *v[4];  // u v w T
 };
 
-// Work list of the deposit: one item per brick, or -- for bricks holding more
-// than kSplitMin particles -- several items, each a slice of the brick's source
-// particles. Items of split bricks come first (largest work first), then the
-// rest; CTAs take items in order from an atomic counter.
-constexpr int kChunkVisits = 32768;   // target particle visits per item
-constexpr int kSplitMin = kChunkVisits / 4;
+// Deposit bricks (the cells one CTA owns) are BR^3 with BR = 16 where the grid
+// allows (every side a multiple of 16, at least 32 cells: the source window of
+// BR + 4 cells must not wrap onto itself), else 8. A brick's source particles
+// (those whose step-start cell lies within two cells of it) are visited about
+// ((BR+4)/BR)^3 times each: 1.95 at BR = 16, 3.4 at BR = 8.
+//
+// Work list of the deposit: one item per deposit brick, or -- for bricks whose
+// source window holds many particles -- several items, each a slice of the
+// brick's source particles. Items of split bricks come first (largest work
+// first), then the rest; CTAs take items in order from an atomic counter.
+template <int BR> struct DepTraits;
+template <> struct DepTraits<8> {
+  static constexpr int kThreads = 256, kChunkVisits = 32768, kVisitFactor = 4;
+};
+template <> struct DepTraits<16> {
+  static constexpr int kThreads = 1024, kChunkVisits = 131072, kVisitFactor = 2;
+};
 constexpr int kMaxChunks = 256;
 
 struct Work {
@@ -73,8 +82,10 @@ struct Work {
   int32_t *n_items;     // device scalar
   int32_t *next;        // device counters, one per deposit launch
   int32_t *done;        // per slot: items finished
-  long long *tiles;     // per slot: 5 x 512 int64
+  long long *tiles;     // per slot: 5 x BR^3 int64
   int64_t slot_cap;
+  int br;               // deposit brick edge, 8 or 16
+  int nbd;              // number of deposit bricks
 };
 
 struct F32Form {
@@ -770,16 +781,32 @@ __device__ inline long long get_fixed(const uint32_t *lo, const uint32_t *hi) {
 
 // accumulator slot of brick-local cell (x,y,z): rows padded by one word so that
 // neighbouring rows do not fall on the same shared-memory banks
-constexpr int kRow = kBr + 1;
-constexpr int kAccSlots = kRow * kBr * kBr;
-__device__ inline int slot_of(int x, int y, int z) { return (z * kBr + y) * kRow + x; }
+template <int BR> struct Acc {
+  static constexpr int kRow = BR + 1, kSlots = kRow * BR * BR;
+  static __device__ __forceinline__ int slot(int x, int y, int z) { return (z * BR + y) * kRow + x; }
+};
 
+// particles whose step-start cell lies in deposit brick b (the sum over its (BR/8)^3 sort bricks)
+template <int BR>
 __global__ void k_work_count(Geom G, const int32_t *__restrict__ cs, Work w, int nb) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb) return;
-  const int32_t nbp = cs[(int64_t)(b + 1) * kBr * kBr * kBr] - cs[(int64_t)b * kBr * kBr * kBr];
+  constexpr int S = BR / kBr, NB3 = kBr * kBr * kBr;
+  const int ndx = G.n[0] / BR, ndy = G.n[1] / BR;
+  const int nbx = G.n[0] / kBr, nby = G.n[1] / kBr;
+  const int dx = b % ndx, dy = (b / ndx) % ndy, dz = b / (ndx * ndy);
+  int64_t nbp = 0;
+#pragma unroll
+  for (int q = 0; q < S * S * S; ++q) {
+    const int sx = dx * S + q % S, sy = dy * S + (q / S) % S, sz = dz * S + q / (S * S);
+    const int64_t sb = ((int64_t)sz * nby + sy) * nbx + sx;
+    nbp += cs[(sb + 1) * NB3] - cs[sb * NB3];
+  }
+  constexpr int64_t kSplitMin = DepTraits<BR>::kChunkVisits / DepTraits<BR>::kVisitFactor;
   int c = 1;
-  if (nbp > kSplitMin) c = min(kMaxChunks, (int)((4ll * nbp + kChunkVisits - 1) / kChunkVisits));
+  if (nbp > kSplitMin)
+    c = (int)min((int64_t)kMaxChunks, (DepTraits<BR>::kVisitFactor * nbp + DepTraits<BR>::kChunkVisits - 1) /
+                                          DepTraits<BR>::kChunkVisits);
   const bool split = c > 1;
   w.cnt_a[b] = split ? c : 0;
   w.cnt_b[b] = split ? 0 : 1;
@@ -808,171 +835,222 @@ __global__ void k_work_fill(Work w, int nb) {
   }
 }
 
-// Deposit into bricks of 8^3 interior cells, one walk over each brick's source
+// add a contribution already scaled to the fixed-point grid (|v| < 2^25) when pred holds
+__device__ __forceinline__ void add_fixed32(uint32_t *lo, uint32_t *hi, int32_t v, bool pred) {
+  if (pred) {
+    const uint32_t vl = (uint32_t)v;
+    const uint32_t old = atomicAdd(lo, vl);
+    // high word: the sign extension plus the carry out of the low word; zero unless a
+    // carry (positive v) or a borrow (negative v) crosses 2^32
+    const uint32_t carry = (old + vl) < old ? 1u : 0u;
+    const uint32_t vh = (uint32_t)(v >> 31) + carry;
+    if (vh) atomicAdd(hi, vh);
+  }
+}
+
+// trilinear deposit (particle.cpp:526-559, :586-658) of a particle at brick-relative cell r3
+// with in-cell offsets o3 and value `val` (already times the field's fixed-point scale):
+// node = cell + h, the 8 cells node - 1 .. node get products of x_l / (1 - x_l)
+template <int BR>
+__device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, const int r3[3], const float o3[3],
+                                                  float val) {
+  float w[3][2];
+  int t0[3];
+  bool ok[3][2];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int hh = o3[d] >= 0.5f;
+    const float xl = o3[d] - hh + 0.5f;
+    t0[d] = r3[d] + hh - 1;  // target of the "1 - x_l" side; t0 + 1 gets x_l
+    w[d][0] = 1.f - xl;
+    w[d][1] = xl;
+    ok[d][0] = (unsigned)t0[d] < (unsigned)BR;
+    ok[d][1] = (unsigned)(t0[d] + 1) < (unsigned)BR;
+  }
+  const int base = Acc<BR>::slot(t0[0], t0[1], t0[2]);
+#pragma unroll
+  for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+      const float wyz = w[2][oz] * w[1][oy] * val;
+      const bool pyz = ok[2][oz] && ok[1][oy];
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const int sl = base + (oz * BR + oy) * Acc<BR>::kRow + ox;
+        const bool pr = pyz && ok[0][ox];
+        add_fixed32(&lo[pr ? sl : 0], &hi[pr ? sl : 0], __float2int_rn(w[0][ox] * wyz), pr);
+      }
+    }
+}
+
+// face-normal deposits (particle.cpp:498-524): along d, face r3[d] gets (1 - x_l) R_d and
+// face r3[d] + 1 gets x_l R_d, at the particle's cell across. lo[d]/hi[d]: field d's words.
+template <int BR>
+__device__ __forceinline__ void deposit_faces(uint32_t *const *lo, uint32_t *const *hi, const int r3[3],
+                                              const float o3[3], const float ru[3], const float *scale) {
+  const bool in0 = (unsigned)r3[0] < (unsigned)BR, in1 = (unsigned)r3[1] < (unsigned)BR,
+             in2 = (unsigned)r3[2] < (unsigned)BR;
+  const bool acr[3] = {in1 && in2, in0 && in2, in0 && in1};
+  const int sl0 = Acc<BR>::slot(r3[0], r3[1], r3[2]);
+  const int step[3] = {1, Acc<BR>::kRow, BR * Acc<BR>::kRow};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float r = ru[d] * scale[1 + d];
+    const bool lo_in = (unsigned)r3[d] < (unsigned)BR, hi_in = (unsigned)(r3[d] + 1) < (unsigned)BR;
+    const bool p0 = acr[d] && lo_in, p1 = acr[d] && hi_in;
+    add_fixed32(&lo[d][p0 ? sl0 : 0], &hi[d][p0 ? sl0 : 0], __float2int_rn((1.f - o3[d]) * r), p0);
+    add_fixed32(&lo[d][p1 ? sl0 + step[d] : 0], &hi[d][p1 ? sl0 + step[d] : 0], __float2int_rn(o3[d] * r), p1);
+  }
+}
+
+// exclusive prefix of n <= 2 * blockDim.x int32 counts in place: a[0..n] (a[n] = total);
+// every thread of the block calls it
+__device__ __forceinline__ void block_exclusive_scan2(int32_t *a, int n, int32_t *warp_sums) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  const int i0 = 2 * t, i1 = 2 * t + 1;
+  const int32_t v0 = i0 < n ? a[i0] : 0, v1 = i1 < n ? a[i1] : 0;
+  int32_t x = v0 + v1;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int32_t ws = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += y;
+    }
+    if (lane < nw) warp_sums[lane] = ws;  // inclusive warp totals
+  }
+  __syncthreads();
+  const int32_t before = (wid ? warp_sums[wid - 1] : 0) + x - (v0 + v1);
+  if (i0 < n) a[i0] = before;
+  if (i1 < n) a[i1] = before + v0;
+  if (t == (int)blockDim.x - 1) a[n] = warp_sums[nw - 1];
+  __syncthreads();
+}
+
+// Shared memory of the deposit CTA for brick edge BR.
+template <int BR, int NF> struct DepSmem {
+  static constexpr int kSeg = 2 + BR / kBr;                 // x segments of a source row
+  static constexpr int kRanges = (BR + 2 * kHalo) * (BR + 2 * kHalo) * kSeg;
+  static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR>::kSlots;
+  static constexpr size_t kBytes = 2 * kAcc + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
+  static_assert(kRanges <= 2 * DepTraits<BR>::kThreads, "ranges exceed the block scan");
+};
+
+// Deposit into bricks of BR^3 interior cells, one walk over each brick's source
 // particles per stage: at the *_int positions the concentration and the face
 // momentum (DO_INT), at the *_new positions RHS_T (DO_NEW). Field slots:
 // 0 C, 1-3 RHS_RU x/y/z, 4 RHS_Part_Temp (scale exponents f.se[0..4]).
-template <bool DO_INT, bool DO_NEW>
-__global__ void __launch_bounds__(kDepThreads) k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w, int twc,
-                                                       double *__restrict__ outC, double *__restrict__ outX,
-                                                       double *__restrict__ outY, double *__restrict__ outZ,
-                                                       double *__restrict__ outE) {
+// The source window (the brick and two cells around it) is a list of row
+// segments, each a run of cells of one sort brick and so a contiguous range of
+// the sorted particles; the CTA's threads stride over the window's particles
+// in order (coalesced), each finding its segment by binary search.
+template <bool DO_INT, bool DO_NEW, int BR>
+__global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w,
+                                                                   int twc, double *__restrict__ outC,
+                                                                   double *__restrict__ outX,
+                                                                   double *__restrict__ outY,
+                                                                   double *__restrict__ outZ,
+                                                                   double *__restrict__ outE) {
   constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
   constexpr int FE = DO_INT ? 4 : 0;  // accumulator index of RHS_Part_Temp
-  constexpr int NS = kSrc * kSrc * kSrc;
-  constexpr int NB3 = kBr * kBr * kBr;
-  __shared__ uint32_t acc_lo[NF][kAccSlots];
-  __shared__ uint32_t acc_hi[NF][kAccSlots];
-  __shared__ int32_t pre[NS + 1];
-  __shared__ int32_t beg[NS];
-  __shared__ int32_t sh_item, sh_last;
-  const int nbx = G.n[0] / kBr, nby = G.n[1] / kBr;
+  constexpr int NB3 = BR * BR * BR;
+  constexpr int SLOTS = Acc<BR>::kSlots;
+  using SM = DepSmem<BR, NF>;
+  constexpr int NR = SM::kRanges, SEG = SM::kSeg, SW = BR + 2 * kHalo;
+  extern __shared__ __align__(16) uint8_t dsm[];
+  uint32_t *acc_lo = reinterpret_cast<uint32_t *>(dsm);
+  uint32_t *acc_hi = acc_lo + NF * SLOTS;
+  int32_t *pre = reinterpret_cast<int32_t *>(acc_hi + NF * SLOTS);  // NR + 1
+  int32_t *beg = pre + NR + 1;                                       // NR
+  int32_t *misc = beg + NR;                                          // 32 warp sums, item, last
+  uint32_t *lo_f[5], *hi_f[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    lo_f[q] = acc_lo + (q < NF ? q : 0) * SLOTS;
+    hi_f[q] = acc_hi + (q < NF ? q : 0) * SLOTS;
+  }
+  const int ndx = G.n[0] / BR, ndy = G.n[1] / BR;
   const int32_t n_items = *w.n_items;
   float scale[5];
 #pragma unroll
   for (int q = 0; q < 5; ++q) scale[q] = ldexpf(1.0f, f.se[q]);  // exact powers of two
   while (true) {
-    if (threadIdx.x == 0) sh_item = atomicAdd(&w.next[0], 1);
+    if (threadIdx.x == 0) misc[32] = atomicAdd(&w.next[0], 1);
     __syncthreads();
-    const int32_t item_idx = sh_item;
+    const int32_t item_idx = misc[32];
     if (item_idx >= n_items) break;
     const int32_t item = w.items[item_idx];
     if (item < 0) { __syncthreads(); continue; }
     const int brick = item >> 8, chunk = item & 255;
     const int nch = w.nchunk[brick];
-    const int bx = (brick % nbx) * kBr, by = ((brick / nbx) % nby) * kBr, bz = (brick / (nbx * nby)) * kBr;
+    const int bx = (brick % ndx) * BR, by = ((brick / ndx) % ndy) * BR, bz = (brick / (ndx * ndy)) * BR;
     const int b3[3] = {bx, by, bz};
-    for (int s = threadIdx.x; s < NF * kAccSlots; s += blockDim.x) {
-      (&acc_lo[0][0])[s] = 0u;
-      (&acc_hi[0][0])[s] = 0u;
+    for (int s = threadIdx.x; s < NF * SLOTS; s += blockDim.x) {
+      acc_lo[s] = 0u;
+      acc_hi[s] = 0u;
     }
-    // source cells [b-2, b+B+2): counts -> exclusive prefix (flat particle index space)
-    for (int s = threadIdx.x; s < NS; s += blockDim.x) {
-      const int lx = s % kSrc, ly = (s / kSrc) % kSrc, lz = s / (kSrc * kSrc);
-      int i = bx - kHalo + lx, j = by - kHalo + ly, k = bz - kHalo + lz;
-      i += i < 0 ? G.n[0] : 0; i -= i >= G.n[0] ? G.n[0] : 0;
+    // source window [b - 2, b + BR + 2) as row segments: segment 0 is x in [b-2, b-1], then
+    // BR/8 sort-brick rows of 8 cells, then [b+BR, b+BR+1]
+    for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+      const int sg = r % SEG, row = r / SEG;
+      int j = by - kHalo + row % SW, k = bz - kHalo + row / SW;
       j += j < 0 ? G.n[1] : 0; j -= j >= G.n[1] ? G.n[1] : 0;
       k += k < 0 ? G.n[2] : 0; k -= k >= G.n[2] ? G.n[2] : 0;
-      const uint32_t id = brick_id(G, i, j, k);
-      const int32_t a0 = f.cell_start[id], e0 = f.cell_start[id + 1];
-      beg[s] = a0;
-      pre[s + 1] = e0 - a0;
-    }
-    if (threadIdx.x == 0) pre[0] = 0;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      int32_t carry = 0;
-      for (int base = 0; base < NS; base += 32) {
-        int idx = base + threadIdx.x + 1;
-        int32_t v = idx <= NS ? pre[idx] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          int32_t y = __shfl_up_sync(0xffffffffu, v, o);
-          if ((int)threadIdx.x >= o) v += y;
-        }
-        if (idx <= NS) pre[idx] = v + carry;
-        carry += __shfl_sync(0xffffffffu, v, 31);
-      }
+      int x0, len;
+      if (sg == 0) { x0 = bx - kHalo; len = kHalo; }
+      else if (sg == SEG - 1) { x0 = bx + BR; len = kHalo; }
+      else { x0 = bx + (sg - 1) * kBr; len = kBr; }
+      x0 += x0 < 0 ? G.n[0] : 0; x0 -= x0 >= G.n[0] ? G.n[0] : 0;
+      const uint32_t id = brick_id(G, x0, j, k);  // the segment's cells are ids id .. id + len - 1
+      const int32_t a0 = f.cell_start[id];
+      beg[r] = a0;
+      pre[r] = f.cell_start[id + len] - a0;
     }
     __syncthreads();
-    const int32_t total = pre[NS];
+    block_exclusive_scan2(pre, NR, misc);
+    const int32_t total = pre[NR];
     const int32_t t0 = (int32_t)(((int64_t)total * chunk) / nch);
     const int32_t t1 = (int32_t)(((int64_t)total * (chunk + 1)) / nch);
     for (int32_t t = t0 + (int32_t)threadIdx.x; t < t1; t += (int32_t)blockDim.x) {
-      // source cell: last s with pre[s] <= t
-      int lo = 0, hi = NS;
+      // segment: last r with pre[r] <= t
+      int lo = 0, hi = NR;
       while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
+        const int mid = (lo + hi) >> 1;
         if (pre[mid] <= t) lo = mid; else hi = mid;
       }
       const int32_t p = beg[lo] + (t - pre[lo]);
       if (DO_INT) {
         const uint32_t c = SI.cell[p];
-        const int c3[3] = {ci_(c), cj_(c), ck_(c)};
         int r3[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) r3[d] = rel_local(c3[d], b3[d], G.n[d]);
+        r3[0] = rel_local(ci_(c), b3[0], G.n[0]);
+        r3[1] = rel_local(cj_(c), b3[1], G.n[1]);
+        r3[2] = rel_local(ck_(c), b3[2], G.n[2]);
         // reachable targets: trilinear cells r3 - 1 .. r3 + 1, faces r3 .. r3 + 1 (normal) and r3 (across)
-        const bool near = r3[0] >= -1 && r3[0] <= kBr && r3[1] >= -1 && r3[1] <= kBr && r3[2] >= -1 && r3[2] <= kBr;
-        if (near) {
+        if (r3[0] >= -1 && r3[0] <= BR && r3[1] >= -1 && r3[1] <= BR && r3[2] >= -1 && r3[2] <= BR) {
           const float o3[3] = {SI.o[0][p], SI.o[1][p], SI.o[2][p]};
-          // trilinear: node = cell + h, targets node - o, factor o ? 1 - x_l : x_l
-          int lt0[3];
-          float xl3[3];
-          bool any = true;
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const int hh = o3[d] >= 0.5f;
-            xl3[d] = o3[d] - hh + 0.5f;
-            lt0[d] = r3[d] + hh;
-            any &= (lt0[d] >= 0) && (lt0[d] - 1 < kBr);
-          }
-          if (any) {
-#pragma unroll
-            for (int o = 0; o < 8; ++o) {
-              const int ox = (o >> 2) & 1, oy = (o >> 1) & 1, oz = o & 1;
-              const int tx = lt0[0] - ox, ty = lt0[1] - oy, tz = lt0[2] - oz;
-              if ((unsigned)tx >= (unsigned)kBr || (unsigned)ty >= (unsigned)kBr || (unsigned)tz >= (unsigned)kBr) continue;
-              const float wt = (ox ? 1.f - xl3[0] : xl3[0]) * (oy ? 1.f - xl3[1] : xl3[1]) * (oz ? 1.f - xl3[2] : xl3[2]);
-              const int sl = slot_of(tx, ty, tz);
-              add_fixed(&acc_lo[0][sl], &acc_hi[0][sl], __float2ll_rn(wt * scale[0]));
-            }
-          }
+          deposit_trilinear<BR>(lo_f[0], hi_f[0], r3, o3, scale[0]);
           if (twc) {
-            // face-normal (particle.cpp:498-524): face c gets (1 - x_l) R, face c + 1 gets x_l R
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-              const int p1 = (d + 1) % 3, p2 = (d + 2) % 3;
-              if ((unsigned)r3[p1] >= (unsigned)kBr || (unsigned)r3[p2] >= (unsigned)kBr) continue;
-              if (r3[d] < -1 || r3[d] >= kBr) continue;
-              const float r = f.rhs_u[d][p];
-              const float xl = o3[d];
-#pragma unroll
-              for (int side = 0; side < 2; ++side) {
-                const int tt = r3[d] + side;
-                if ((unsigned)tt >= (unsigned)kBr) continue;
-                int l3[3];
-                l3[d] = tt; l3[p1] = r3[p1]; l3[p2] = r3[p2];
-                const float wt = side ? xl * r : (1.f - xl) * r;
-                const int sl = slot_of(l3[0], l3[1], l3[2]);
-                add_fixed(&acc_lo[1 + d][sl], &acc_hi[1 + d][sl], __float2ll_rn(wt * scale[1 + d]));
-              }
-            }
+            const float ru[3] = {f.rhs_u[0][p], f.rhs_u[1][p], f.rhs_u[2][p]};
+            deposit_faces<BR>(&lo_f[1], &hi_f[1], r3, o3, ru, scale);
           }
         }
       }
       if (DO_NEW) {
         const uint32_t c = SN.cell[p];
-        const int c3[3] = {ci_(c), cj_(c), ck_(c)};
         int r3[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) r3[d] = rel_local(c3[d], b3[d], G.n[d]);
-        const bool near = r3[0] >= -1 && r3[0] <= kBr && r3[1] >= -1 && r3[1] <= kBr && r3[2] >= -1 && r3[2] <= kBr;
-        if (near) {
+        r3[0] = rel_local(ci_(c), b3[0], G.n[0]);
+        r3[1] = rel_local(cj_(c), b3[1], G.n[1]);
+        r3[2] = rel_local(ck_(c), b3[2], G.n[2]);
+        if (r3[0] >= -1 && r3[0] <= BR && r3[1] >= -1 && r3[1] <= BR && r3[2] >= -1 && r3[2] <= BR) {
           const float o3[3] = {SN.o[0][p], SN.o[1][p], SN.o[2][p]};
-          int lt0[3];
-          float xl3[3];
-          bool any = true;
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const int hh = o3[d] >= 0.5f;
-            xl3[d] = o3[d] - hh + 0.5f;
-            lt0[d] = r3[d] + hh;
-            any &= (lt0[d] >= 0) && (lt0[d] - 1 < kBr);
-          }
-          if (any) {
-            const float val = f.rhs_t[p];
-#pragma unroll
-            for (int o = 0; o < 8; ++o) {
-              const int ox = (o >> 2) & 1, oy = (o >> 1) & 1, oz = o & 1;
-              const int tx = lt0[0] - ox, ty = lt0[1] - oy, tz = lt0[2] - oz;
-              if ((unsigned)tx >= (unsigned)kBr || (unsigned)ty >= (unsigned)kBr || (unsigned)tz >= (unsigned)kBr) continue;
-              const float wt =
-                  (ox ? 1.f - xl3[0] : xl3[0]) * (oy ? 1.f - xl3[1] : xl3[1]) * (oz ? 1.f - xl3[2] : xl3[2]) * val;
-              const int sl = slot_of(tx, ty, tz);
-              add_fixed(&acc_lo[FE][sl], &acc_hi[FE][sl], __float2ll_rn(wt * scale[4]));
-            }
-          }
+          deposit_trilinear<BR>(lo_f[FE], hi_f[FE], r3, o3, f.rhs_t[p] * scale[4]);
         }
       }
     }
@@ -983,44 +1061,45 @@ __global__ void __launch_bounds__(kDepThreads) k_dep32(Geom G, F32Form f, Set32 
       long long *tile = w.tiles + (int64_t)slot * 5 * NB3;
       for (int s = threadIdx.x; s < NF * NB3; s += blockDim.x) {
         const int q = s / NB3, r = s % NB3;
-        const int sl = slot_of(r % kBr, (r / kBr) % kBr, r / (kBr * kBr));
-        const long long v = get_fixed(&acc_lo[q][sl], &acc_hi[q][sl]);
+        const int sl = q * SLOTS + Acc<BR>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
+        const long long v = get_fixed(&acc_lo[sl], &acc_hi[sl]);
         if (v) atomicAdd((unsigned long long *)&tile[s], (unsigned long long)v);
       }
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) sh_last = (atomicAdd(&w.done[slot], 1) == nch - 1);
+      if (threadIdx.x == 0) misc[33] = (atomicAdd(&w.done[slot], 1) == nch - 1);
       __syncthreads();
-      if (sh_last) {
+      const int last = misc[33];
+      if (last) {
         __threadfence();
         for (int s = threadIdx.x; s < NF * NB3; s += blockDim.x) {
           const int q = s / NB3, r = s % NB3;
-          const int sl = slot_of(r % kBr, (r / kBr) % kBr, r / (kBr * kBr));
+          const int sl = q * SLOTS + Acc<BR>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
           const unsigned long long v = (unsigned long long)__ldcg(&tile[s]);
-          acc_lo[q][sl] = (uint32_t)v;
-          acc_hi[q][sl] = (uint32_t)(v >> 32);
+          acc_lo[sl] = (uint32_t)v;
+          acc_hi[sl] = (uint32_t)(v >> 32);
           tile[s] = 0;  // ready for the next launch
         }
         if (threadIdx.x == 0) w.done[slot] = 0;
       }
       __syncthreads();
-      if (!sh_last) continue;
+      if (!last) continue;
     }
     for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
-      const int lx = s % kBr, ly = (s / kBr) % kBr, lz = s / (kBr * kBr);
+      const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
       const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
-      const int sl = slot_of(lx, ly, lz);
+      const int sl = Acc<BR>::slot(lx, ly, lz);
       if (DO_INT) {
-        outC[g] = fixed_to_f64(get_fixed(&acc_lo[0][sl], &acc_hi[0][sl]), f.se[0]);
+        outC[g] = fixed_to_f64(get_fixed(&lo_f[0][sl], &hi_f[0][sl]), f.se[0]);
         if (twc) {
-          outX[g] = fixed_to_f64(get_fixed(&acc_lo[1][sl], &acc_hi[1][sl]), f.se[1]);
-          outY[g] = fixed_to_f64(get_fixed(&acc_lo[2][sl], &acc_hi[2][sl]), f.se[2]);
-          outZ[g] = fixed_to_f64(get_fixed(&acc_lo[3][sl], &acc_hi[3][sl]), f.se[3]);
+          outX[g] = fixed_to_f64(get_fixed(&lo_f[1][sl], &hi_f[1][sl]), f.se[1]);
+          outY[g] = fixed_to_f64(get_fixed(&lo_f[2][sl], &hi_f[2][sl]), f.se[2]);
+          outZ[g] = fixed_to_f64(get_fixed(&lo_f[3][sl], &hi_f[3][sl]), f.se[3]);
         } else {
           outX[g] = 0.0; outY[g] = 0.0; outZ[g] = 0.0;
         }
       }
-      if (DO_NEW) outE[g] = fixed_to_f64(get_fixed(&acc_lo[FE][sl], &acc_hi[FE][sl]), f.se[4]);
+      if (DO_NEW) outE[g] = fixed_to_f64(get_fixed(&lo_f[FE][sl], &hi_f[FE][sl]), f.se[4]);
     }
     __syncthreads();
   }
@@ -1207,8 +1286,11 @@ int sort_step(pstep_ctx *h) {
   }
   {  // deposit work list for this step's particle distribution
     Work &w = f.work;
-    const int nbk = (G.n[0] / kBr) * (G.n[1] / kBr) * (G.n[2] / kBr);
-    k_work_count<<<nb(nbk), kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+    const int nbk = w.nbd;
+    if (w.br == 16)
+      k_work_count<16><<<nb(nbk), kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+    else
+      k_work_count<8><<<nb(nbk), kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
     PSTEP_LAUNCHED(h);
     TRY32(exclusive_scan(h, w.cnt_a, nbk, w.off_a, nullptr));
     TRY32(exclusive_scan(h, w.cnt_b, nbk, w.off_b, nullptr));
@@ -1257,8 +1339,15 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->tmpf, cap));
   {  // deposit work list
     Work &w = f->work;
-    const int64_t nbk = (int64_t)(G.n[0] / kBr) * (G.n[1] / kBr) * (G.n[2] / kBr);
-    w.slot_cap = (int64_t)h->cap / kSplitMin + 1;
+    w.br = 16;
+    for (int d = 0; d < 3; ++d)
+      if (G.n[d] % 16 != 0 || G.n[d] < 32) w.br = 8;
+    const int64_t nbk = (int64_t)(G.n[0] / w.br) * (G.n[1] / w.br) * (G.n[2] / w.br);
+    w.nbd = (int)nbk;
+    const int64_t split_min = w.br == 16 ? DepTraits<16>::kChunkVisits / DepTraits<16>::kVisitFactor
+                                         : DepTraits<8>::kChunkVisits / DepTraits<8>::kVisitFactor;
+    w.slot_cap = (int64_t)h->cap / split_min + 1;
+    const int64_t br3 = (int64_t)w.br * w.br * w.br;
     TRY32(dalloc32(h, w.items, (size_t)(nbk + 2 * w.slot_cap * 2 + 64)));
     TRY32(dalloc32(h, w.nchunk, (size_t)nbk));
     TRY32(dalloc32(h, w.slot, (size_t)nbk));
@@ -1267,9 +1356,9 @@ int f32_create(pstep_ctx *h) {
     TRY32(dalloc32(h, w.n_items, 1));
     TRY32(dalloc32(h, w.next, 64));
     TRY32(dalloc32(h, w.done, (size_t)w.slot_cap));
-    TRY32(dalloc32(h, w.tiles, (size_t)w.slot_cap * 5 * kBr * kBr * kBr));
+    TRY32(dalloc32(h, w.tiles, (size_t)(w.slot_cap * 5 * br3)));
     PSTEP_CUDA(cudaMemsetAsync(w.done, 0, sizeof(int32_t) * w.slot_cap, h->stream));
-    PSTEP_CUDA(cudaMemsetAsync(w.tiles, 0, sizeof(long long) * w.slot_cap * 5 * kBr * kBr * kBr, h->stream));
+    PSTEP_CUDA(cudaMemsetAsync(w.tiles, 0, sizeof(long long) * w.slot_cap * 5 * br3, h->stream));
     PSTEP_CUDA(cudaMemsetAsync(w.n_items, 0, sizeof(int32_t), h->stream));
   }
   TRY32(dalloc32(h, f->bounds, 8));
@@ -1565,23 +1654,48 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
 }
 
 namespace {
+// one launch of the deposit variant for (do_int, do_new) with brick edge BR:
+// persistent CTAs (as many as fit on the SMs) pulling work items
+template <bool DO_INT, bool DO_NEW, int BR>
+int dep_run1(pstep_ctx *h, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z, double *E) {
+  constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
+  constexpr size_t smem = DepSmem<BR, NF>::kBytes;
+  auto kern = k_dep32<DO_INT, DO_NEW, BR>;
+  PSTEP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PSTEP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, DepTraits<BR>::kThreads, smem));
+  if (per_sm < 1) {
+    snprintf(h->err, sizeof h->err, "deposit kernel does not fit on an SM (%zu B shared memory)", smem);
+    return PSTEP_ERR_CUDA;
+  }
+  F32Form &f = *h->f32;
+  kern<<<h->num_sms * per_sm, DepTraits<BR>::kThreads, smem, h->stream>>>(h->geom, f, SI, SN, f.work, h->cfg.twc,
+                                                                           C, X, Y, Z, E);
+  PSTEP_LAUNCHED(h);
+  return PSTEP_OK;
+}
+
+template <int BR>
+int dep_run(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z,
+            double *E) {
+  if (do_int && do_new) return dep_run1<true, true, BR>(h, SI, SN, C, X, Y, Z, E);
+  if (do_int) return dep_run1<true, false, BR>(h, SI, SN, C, X, Y, Z, E);
+  return dep_run1<false, true, BR>(h, SI, SN, C, X, Y, Z, E);
+}
+
 int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   F32Form &f = *h->f32;
   const Geom &G = h->geom;
   k_scales<<<1, 32, 0, h->stream>>>(f);  // fold this advance's maxima into the fixed-point scales
   PSTEP_LAUNCHED(h);
-  const int grid = h->num_sms * 8;  // persistent CTAs pulling work items
   PSTEP_CUDA(cudaMemsetAsync(f.work.next, 0, sizeof(int32_t), h->stream));
   double *C = h->dep[PSTEP_FIELD_C], *X = h->dep[PSTEP_FIELD_RU_X], *Y = h->dep[PSTEP_FIELD_RU_Y],
          *Z = h->dep[PSTEP_FIELD_RU_Z], *E = h->dep[PSTEP_FIELD_PART_TEMP];
-  if (do_int && do_new) {
-    k_dep32<true, true><<<grid, kDepThreads, 0, h->stream>>>(G, f, SI, SN, f.work, h->cfg.twc, C, X, Y, Z, E);
-  } else if (do_int) {
-    k_dep32<true, false><<<grid, kDepThreads, 0, h->stream>>>(G, f, SI, SN, f.work, h->cfg.twc, C, X, Y, Z, E);
+  if (f.work.br == 16) {
+    TRY32(dep_run<16>(h, do_int, do_new, SI, SN, C, X, Y, Z, E));
   } else {
-    k_dep32<false, true><<<grid, kDepThreads, 0, h->stream>>>(G, f, SI, SN, f.work, h->cfg.twc, C, X, Y, Z, E);
+    TRY32(dep_run<8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E));
   }
-  PSTEP_LAUNCHED(h);
   // interior values are final (periodic targets): refresh the ghost layers only
   if (do_int) {
     double *all[4] = {C, X, Y, Z};
