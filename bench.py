@@ -150,7 +150,7 @@ def peaks():
 
 def make_inputs(wl):
     t0 = time.time()
-    case = gen.make_case(wl.n, wl.n_particles, wl.seed, wl.clustered)
+    case = gen.make_case(wl.n, wl.n_particles, wl.seed, wl.clustered, nblobs=wl.nblobs)
     bp = config.box_params(wl.n, wl.n_particles, dp_over_dx=wl.dp_over_dx, mass_loading=wl.mass_loading)
     fields = [gen.ghost(case[k]) for k in ("ux", "uy", "uz", "T")]
     return case, bp, fields, time.time() - t0
@@ -411,7 +411,7 @@ def main():
             "config": {"workload": wl.name, "cells": wl.n ** 3, "particles": n, "form": args.form,
                        "learned_correction": corr_model is not None, "dp_over_dx": wl.dp_over_dx,
                        "mass_loading": wl.mass_loading,
-                       "order_tracking": bool(flags & pstep.TRACK_ORDER), "clustered": wl.clustered,
+                       "order_tracking": bool(flags & pstep.TRACK_ORDER), "clustered": wl.clustered, "blobs": wl.nblobs if wl.clustered else 0,
                        "l2": "inputs larger than L2 (particle state alone is several GB)",
                        "parallelism": f"replicas x{world}", "input_generation_s": round(gen_s, 2)},
             "roofline": roof, "phases": phases, "fp32_plain": fp32_plain, "fp64_dropin": fp64, "cpu_baseline": cpu,

@@ -120,6 +120,7 @@ class Workload:
     seed: int
     dp_over_dx: float = 0.1
     mass_loading: float = 0.2
+    nblobs: int = 64  # Gaussian blobs holding the clustered half of the particles (sigma 4 cells)
 
 
 # Seeded synthetic stand-ins for the reference's run shapes.
@@ -129,6 +130,11 @@ WORKLOADS = {
     "box512_clustered": Workload("box512_clustered", 512, 1 << 27, True, 1, 1003),
     # the corrected-step workload: larger, heavier particles (d_p/dx 0.5, mass loading 1.0)
     "box512_corrected": Workload("box512_corrected", 512, 1 << 27, True, 100, 1004, 0.5, 1.0),
+    # box512_corrected at 1/8 of the cells and particles with 8 blobs instead of 64: each
+    # blob holds 2^20 particles as there, so the cell occupancy (up to ~1000 particles
+    # in a blob-centre cell, 44% of the particles in cells holding 64 or more) is the
+    # same; the profiling case for the deposit
+    "box256_dense": Workload("box256_dense", 256, 1 << 24, True, 1, 1005, 0.5, 1.0, 8),
 }
 
 

@@ -62,20 +62,21 @@ struct Set32 {
 // ((BR+4)/BR)^3 times each: 1.95 at BR = 16, 3.4 at BR = 8.
 //
 // Work list of the deposit: one item per deposit brick, or -- for bricks whose
-// source window holds many particles -- several items, each a slice of the
-// brick's source particles. Items of split bricks come first (largest work
-// first), then the rest; CTAs take items in order from an atomic counter.
+// source window holds more than kChunkMax particles -- several items, each a
+// slice of at most kChunkMax of the window's particles. Items of split bricks
+// come first (largest work first), then the rest; CTAs take items in order from
+// an atomic counter. kVisit bounds the visits per particle (windows overlap), so
+// at most kVisit * particles / kChunkMax bricks split.
 template <int BR> struct DepTraits;
 template <> struct DepTraits<8> {
-  static constexpr int kThreads = 256, kChunkVisits = 32768, kVisitFactor = 4;
+  static constexpr int kThreads = 256, kVisit = 4;  // (12/8)^3 = 3.4
 };
 template <> struct DepTraits<16> {
-  static constexpr int kThreads = 1024, kChunkVisits = 131072, kVisitFactor = 2;
+  static constexpr int kThreads = 1024, kVisit = 2;  // (20/16)^3 = 1.95
 };
-constexpr int kMaxChunks = 256;
 
 struct Work {
-  int32_t *items;       // (brick << 8) | chunk
+  long long *items;     // (brick << 32) | chunk, or -1 (skip)
   int32_t *nchunk;      // per brick
   int32_t *slot;        // per brick: index of its global tile, or -1
   int32_t *cnt_a, *cnt_b, *cnt_s, *off_a, *off_b, *off_s;  // per brick (+1) scan arrays
@@ -86,6 +87,7 @@ struct Work {
   int64_t slot_cap;
   int br;               // deposit brick edge, 8 or 16
   int nbd;              // number of deposit bricks
+  int32_t *err;         // device error word (kErrCapacity)
 };
 
 struct F32Form {
@@ -761,22 +763,23 @@ __device__ inline int rel_local(int c, int b, int n) {
 
 // Exact sums with 32-bit shared-memory atomics. Every contribution is scaled so
 // that the largest magnitude is 2^24 (the fp32 values carry 24 significant bits,
-// so nothing beyond their own rounding is lost) and rounded to a 64-bit integer
-// of magnitude below 2^25. A slot holds the two's-complement sum in two 32-bit
-// words: the low word is added with its old value returned, and the high word
-// changes only on a carry or borrow out of the low word (rare at this size:
-// about once per 2^7 or more adds). The pair is the exact sum modulo 2^64,
-// whatever the order of the adds.
-__device__ inline void add_fixed(uint32_t *lo, uint32_t *hi, long long v) {
-  const unsigned long long u = (unsigned long long)v;
-  const uint32_t vl = (uint32_t)u;
-  const uint32_t vh = (uint32_t)(u >> 32);
-  const uint32_t old = atomicAdd(lo, vl);
-  const uint32_t carry = (uint32_t)(old + vl) < old ? 1u : 0u;
-  if (vh + carry) atomicAdd(hi, vh + carry);
+// so nothing beyond their own rounding is lost) and rounded to an integer v with
+// |v| < 2^25. A slot holds two 32-bit words: the low word sums v mod 2^16
+// (unsigned, below 2^16 each), the high word sums v >> 16 (signed, |.| < 2^9).
+// Both adds are fire-and-forget (no returned value, no carry handling). The low
+// word cannot wrap while a slot receives at most 2^16 contributions, and a slot
+// receives at most one per particle the work item visits: work items visit at
+// most kChunkMax = 2^16 particles. The sum is hi * 2^16 + lo, exact whatever the
+// order of the adds.
+constexpr int32_t kChunkMax = 1 << 16;
+__device__ __forceinline__ void add_fixed32(uint32_t *lo, uint32_t *hi, int32_t v, bool pred) {
+  if (pred) {
+    atomicAdd(lo, (uint32_t)v & 0xffffu);
+    atomicAdd(hi, (uint32_t)(v >> 16));
+  }
 }
-__device__ inline long long get_fixed(const uint32_t *lo, const uint32_t *hi) {
-  return (long long)(((unsigned long long)*hi << 32) | (unsigned long long)*lo);
+__device__ __forceinline__ long long get_fixed(const uint32_t *lo, const uint32_t *hi) {
+  return (long long)(int32_t)*hi * 65536ll + (long long)*lo;
 }
 
 // accumulator slot of brick-local cell (x,y,z): rows padded by one word so that
@@ -786,32 +789,54 @@ template <int BR> struct Acc {
   static __device__ __forceinline__ int slot(int x, int y, int z) { return (z * BR + y) * kRow + x; }
 };
 
-// particles whose step-start cell lies in deposit brick b (the sum over its (BR/8)^3 sort bricks)
+// The source window of the deposit brick at (bx, by, bz) -- its cells and two
+// around them -- as SW^2 x SEG row segments: per (y, z) row, x in [b-2, b-1], then
+// BR/8 runs of 8 cells, then [b+BR, b+BR+1]. Each segment lies in one 8^3 sort
+// brick along one x-row, so its particles are one contiguous range
+// [cell_start[id], cell_start[id + len]) of the sorted order.
+template <int BR> struct Window {
+  static constexpr int kSeg = 2 + BR / kBr, kSide = BR + 2 * kHalo, kRanges = kSide * kSide * kSeg;
+  static __device__ __forceinline__ void segment(const Geom &G, int bx, int by, int bz, int r, uint32_t &id,
+                                                 int &len) {
+    const int sg = r % kSeg, row = r / kSeg;
+    int j = by - kHalo + row % kSide, k = bz - kHalo + row / kSide;
+    j += j < 0 ? G.n[1] : 0; j -= j >= G.n[1] ? G.n[1] : 0;
+    k += k < 0 ? G.n[2] : 0; k -= k >= G.n[2] ? G.n[2] : 0;
+    int x0;
+    if (sg == 0) { x0 = bx - kHalo; len = kHalo; }
+    else if (sg == kSeg - 1) { x0 = bx + BR; len = kHalo; }
+    else { x0 = bx + (sg - 1) * kBr; len = kBr; }
+    x0 += x0 < 0 ? G.n[0] : 0; x0 -= x0 >= G.n[0] ? G.n[0] : 0;
+    id = brick_id(G, x0, j, k);
+  }
+};
+
+// per deposit brick: the particles of its source window (one warp per brick) and
+// from that the number of work items, each at most kChunkMax particles
 template <int BR>
 __global__ void k_work_count(Geom G, const int32_t *__restrict__ cs, Work w, int nb) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  constexpr int S = BR / kBr, NB3 = kBr * kBr * kBr;
+  const int lane = threadIdx.x & 31;
+  const int b = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (b >= nb) return;  // whole warps
   const int ndx = G.n[0] / BR, ndy = G.n[1] / BR;
-  const int nbx = G.n[0] / kBr, nby = G.n[1] / kBr;
-  const int dx = b % ndx, dy = (b / ndx) % ndy, dz = b / (ndx * ndy);
-  int64_t nbp = 0;
-#pragma unroll
-  for (int q = 0; q < S * S * S; ++q) {
-    const int sx = dx * S + q % S, sy = dy * S + (q / S) % S, sz = dz * S + q / (S * S);
-    const int64_t sb = ((int64_t)sz * nby + sy) * nbx + sx;
-    nbp += cs[(sb + 1) * NB3] - cs[sb * NB3];
+  const int bx = (b % ndx) * BR, by = ((b / ndx) % ndy) * BR, bz = (b / (ndx * ndy)) * BR;
+  long long total = 0;
+  for (int r = lane; r < Window<BR>::kRanges; r += 32) {
+    uint32_t id;
+    int len;
+    Window<BR>::segment(G, bx, by, bz, r, id, len);
+    total += cs[id + len] - cs[id];
   }
-  constexpr int64_t kSplitMin = DepTraits<BR>::kChunkVisits / DepTraits<BR>::kVisitFactor;
-  int c = 1;
-  if (nbp > kSplitMin)
-    c = (int)min((int64_t)kMaxChunks, (DepTraits<BR>::kVisitFactor * nbp + DepTraits<BR>::kChunkVisits - 1) /
-                                          DepTraits<BR>::kChunkVisits);
-  const bool split = c > 1;
-  w.cnt_a[b] = split ? c : 0;
-  w.cnt_b[b] = split ? 0 : 1;
-  w.cnt_s[b] = split ? 1 : 0;
-  w.nchunk[b] = c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+  if (lane == 0) {
+    const int c = (int)((total + kChunkMax - 1) / kChunkMax);
+    const bool split = c > 1;
+    w.cnt_a[b] = split ? c : 0;
+    w.cnt_b[b] = split ? 0 : 1;
+    w.cnt_s[b] = split ? 1 : 0;
+    w.nchunk[b] = split ? c : 1;
+  }
 }
 
 __global__ void k_work_fill(Work w, int nb) {
@@ -820,31 +845,16 @@ __global__ void k_work_fill(Work w, int nb) {
   if (b == 0) *w.n_items = total_a + w.off_b[nb];
   if (b >= nb) return;
   const int c = w.nchunk[b];
-  if (c > 1 && w.off_s[b] < w.slot_cap) {
-    w.slot[b] = w.off_s[b];
-    for (int q = 0; q < c; ++q) w.items[w.off_a[b] + q] = (b << 8) | q;
+  if (c > 1) {
+    // the slot count bounds the split bricks (see f32_create); a brick past it is
+    // reported and left out rather than run as one oversized item
+    const bool ok = w.off_s[b] < w.slot_cap;
+    w.slot[b] = ok ? w.off_s[b] : -1;
+    for (int q = 0; q < c; ++q) w.items[w.off_a[b] + q] = ok ? ((long long)b << 32 | q) : -1ll;
+    if (!ok) atomicOr(w.err, kErrCapacity);
   } else {
-    if (c > 1) {  // no tile left: run the brick as one item (slower, same result)
-      w.nchunk[b] = 1;
-      for (int q = 1; q < c; ++q) w.items[w.off_a[b] + q] = -1;
-      w.items[w.off_a[b]] = (b << 8);
-    } else {
-      w.items[total_a + w.off_b[b]] = (b << 8);
-    }
+    w.items[total_a + w.off_b[b]] = (long long)b << 32;
     w.slot[b] = -1;
-  }
-}
-
-// add a contribution already scaled to the fixed-point grid (|v| < 2^25) when pred holds
-__device__ __forceinline__ void add_fixed32(uint32_t *lo, uint32_t *hi, int32_t v, bool pred) {
-  if (pred) {
-    const uint32_t vl = (uint32_t)v;
-    const uint32_t old = atomicAdd(lo, vl);
-    // high word: the sign extension plus the carry out of the low word; zero unless a
-    // carry (positive v) or a borrow (negative v) crosses 2^32
-    const uint32_t carry = (old + vl) < old ? 1u : 0u;
-    const uint32_t vh = (uint32_t)(v >> 31) + carry;
-    if (vh) atomicAdd(hi, vh);
   }
 }
 
@@ -877,8 +887,7 @@ __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, co
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) {
         const int sl = base + (oz * BR + oy) * Acc<BR>::kRow + ox;
-        const bool pr = pyz && ok[0][ox];
-        add_fixed32(&lo[pr ? sl : 0], &hi[pr ? sl : 0], __float2int_rn(w[0][ox] * wyz), pr);
+        add_fixed32(lo + sl, hi + sl, __float2int_rn(w[0][ox] * wyz), pyz && ok[0][ox]);
       }
     }
 }
@@ -897,9 +906,8 @@ __device__ __forceinline__ void deposit_faces(uint32_t *const *lo, uint32_t *con
   for (int d = 0; d < 3; ++d) {
     const float r = ru[d] * scale[1 + d];
     const bool lo_in = (unsigned)r3[d] < (unsigned)BR, hi_in = (unsigned)(r3[d] + 1) < (unsigned)BR;
-    const bool p0 = acr[d] && lo_in, p1 = acr[d] && hi_in;
-    add_fixed32(&lo[d][p0 ? sl0 : 0], &hi[d][p0 ? sl0 : 0], __float2int_rn((1.f - o3[d]) * r), p0);
-    add_fixed32(&lo[d][p1 ? sl0 + step[d] : 0], &hi[d][p1 ? sl0 + step[d] : 0], __float2int_rn(o3[d] * r), p1);
+    add_fixed32(lo[d] + sl0, hi[d] + sl0, __float2int_rn((1.f - o3[d]) * r), acr[d] && lo_in);
+    add_fixed32(lo[d] + sl0 + step[d], hi[d] + sl0 + step[d], __float2int_rn(o3[d] * r), acr[d] && hi_in);
   }
 }
 
@@ -936,8 +944,7 @@ __device__ __forceinline__ void block_exclusive_scan2(int32_t *a, int n, int32_t
 
 // Shared memory of the deposit CTA for brick edge BR.
 template <int BR, int NF> struct DepSmem {
-  static constexpr int kSeg = 2 + BR / kBr;                 // x segments of a source row
-  static constexpr int kRanges = (BR + 2 * kHalo) * (BR + 2 * kHalo) * kSeg;
+  static constexpr int kRanges = Window<BR>::kRanges;
   static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR>::kSlots;
   static constexpr size_t kBytes = 2 * kAcc + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
   static_assert(kRanges <= 2 * DepTraits<BR>::kThreads, "ranges exceed the block scan");
@@ -947,10 +954,8 @@ template <int BR, int NF> struct DepSmem {
 // particles per stage: at the *_int positions the concentration and the face
 // momentum (DO_INT), at the *_new positions RHS_T (DO_NEW). Field slots:
 // 0 C, 1-3 RHS_RU x/y/z, 4 RHS_Part_Temp (scale exponents f.se[0..4]).
-// The source window (the brick and two cells around it) is a list of row
-// segments, each a run of cells of one sort brick and so a contiguous range of
-// the sorted particles; the CTA's threads stride over the window's particles
-// in order (coalesced), each finding its segment by binary search.
+// Each thread finds a particle's row segment by binary search over the
+// segments' prefix counts.
 template <bool DO_INT, bool DO_NEW, int BR>
 __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w,
                                                                    int twc, double *__restrict__ outC,
@@ -962,8 +967,7 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
   constexpr int FE = DO_INT ? 4 : 0;  // accumulator index of RHS_Part_Temp
   constexpr int NB3 = BR * BR * BR;
   constexpr int SLOTS = Acc<BR>::kSlots;
-  using SM = DepSmem<BR, NF>;
-  constexpr int NR = SM::kRanges, SEG = SM::kSeg, SW = BR + 2 * kHalo;
+  constexpr int NR = Window<BR>::kRanges;
   extern __shared__ __align__(16) uint8_t dsm[];
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(dsm);
   uint32_t *acc_hi = acc_lo + NF * SLOTS;
@@ -976,6 +980,7 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     lo_f[q] = acc_lo + (q < NF ? q : 0) * SLOTS;
     hi_f[q] = acc_hi + (q < NF ? q : 0) * SLOTS;
   }
+  double *const outs[5] = {outC, outX, outY, outZ, outE};
   const int ndx = G.n[0] / BR, ndy = G.n[1] / BR;
   const int32_t n_items = *w.n_items;
   float scale[5];
@@ -986,9 +991,9 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     __syncthreads();
     const int32_t item_idx = misc[32];
     if (item_idx >= n_items) break;
-    const int32_t item = w.items[item_idx];
+    const long long item = w.items[item_idx];
     if (item < 0) { __syncthreads(); continue; }
-    const int brick = item >> 8, chunk = item & 255;
+    const int brick = (int)(item >> 32), chunk = (int)(item & 0xffffffffll);
     const int nch = w.nchunk[brick];
     const int bx = (brick % ndx) * BR, by = ((brick / ndx) % ndy) * BR, bz = (brick / (ndx * ndy)) * BR;
     const int b3[3] = {bx, by, bz};
@@ -996,19 +1001,10 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
       acc_lo[s] = 0u;
       acc_hi[s] = 0u;
     }
-    // source window [b - 2, b + BR + 2) as row segments: segment 0 is x in [b-2, b-1], then
-    // BR/8 sort-brick rows of 8 cells, then [b+BR, b+BR+1]
     for (int r = threadIdx.x; r < NR; r += blockDim.x) {
-      const int sg = r % SEG, row = r / SEG;
-      int j = by - kHalo + row % SW, k = bz - kHalo + row / SW;
-      j += j < 0 ? G.n[1] : 0; j -= j >= G.n[1] ? G.n[1] : 0;
-      k += k < 0 ? G.n[2] : 0; k -= k >= G.n[2] ? G.n[2] : 0;
-      int x0, len;
-      if (sg == 0) { x0 = bx - kHalo; len = kHalo; }
-      else if (sg == SEG - 1) { x0 = bx + BR; len = kHalo; }
-      else { x0 = bx + (sg - 1) * kBr; len = kBr; }
-      x0 += x0 < 0 ? G.n[0] : 0; x0 -= x0 >= G.n[0] ? G.n[0] : 0;
-      const uint32_t id = brick_id(G, x0, j, k);  // the segment's cells are ids id .. id + len - 1
+      uint32_t id;
+      int len;
+      Window<BR>::segment(G, bx, by, bz, r, id, len);
       const int32_t a0 = f.cell_start[id];
       beg[r] = a0;
       pre[r] = f.cell_start[id + len] - a0;
@@ -1018,7 +1014,16 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     const int32_t total = pre[NR];
     const int32_t t0 = (int32_t)(((int64_t)total * chunk) / nch);
     const int32_t t1 = (int32_t)(((int64_t)total * (chunk + 1)) / nch);
-    for (int32_t t = t0 + (int32_t)threadIdx.x; t < t1; t += (int32_t)blockDim.x) {
+    // Lane groups of 8 walk their own sub-range of the slice, 8 consecutive
+    // particles per pass (one 32-byte sector of each 4-byte array), and the 4
+    // groups of a warp take sub-ranges a quarter of the slice apart. Sorted
+    // particles in a dense cell would otherwise put all 32 lanes of a warp on the
+    // same accumulator slots, where the shared-memory atomics serialise.
+    const int ngroups = (int)blockDim.x >> 3;
+    const int grp = (int)(threadIdx.x >> 5) + ((int)blockDim.x >> 5) * (int)((threadIdx.x >> 3) & 3);
+    const int32_t g0 = t0 + (int32_t)(((int64_t)(t1 - t0) * grp) / ngroups);
+    const int32_t g1 = t0 + (int32_t)(((int64_t)(t1 - t0) * (grp + 1)) / ngroups);
+    for (int32_t t = g0 + (int32_t)(threadIdx.x & 7); t < g1; t += 8) {
       // segment: last r with pre[r] <= t
       int lo = 0, hi = NR;
       while (hi - lo > 1) {
@@ -1056,9 +1061,9 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     }
     __syncthreads();
     const int slot = nch > 1 ? w.slot[brick] : -1;
-    if (slot >= 0) {
-      // split brick: add this slice into the brick's global tile; the last slice converts
-      long long *tile = w.tiles + (int64_t)slot * 5 * NB3;
+    long long *tile = slot >= 0 ? w.tiles + (int64_t)slot * 5 * NB3 : nullptr;
+    if (tile) {
+      // split brick: add this slice into the brick's global tile; the last slice writes the cells
       for (int s = threadIdx.x; s < NF * NB3; s += blockDim.x) {
         const int q = s / NB3, r = s % NB3;
         const int sl = q * SLOTS + Acc<BR>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
@@ -1070,37 +1075,28 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
       if (threadIdx.x == 0) misc[33] = (atomicAdd(&w.done[slot], 1) == nch - 1);
       __syncthreads();
       const int last = misc[33];
-      if (last) {
-        __threadfence();
-        for (int s = threadIdx.x; s < NF * NB3; s += blockDim.x) {
-          const int q = s / NB3, r = s % NB3;
-          const int sl = q * SLOTS + Acc<BR>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
-          const unsigned long long v = (unsigned long long)__ldcg(&tile[s]);
-          acc_lo[sl] = (uint32_t)v;
-          acc_hi[sl] = (uint32_t)(v >> 32);
-          tile[s] = 0;  // ready for the next launch
-        }
-        if (threadIdx.x == 0) w.done[slot] = 0;
-      }
-      __syncthreads();
       if (!last) continue;
+      __threadfence();
     }
     for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
       const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
       const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
       const int sl = Acc<BR>::slot(lx, ly, lz);
-      if (DO_INT) {
-        outC[g] = fixed_to_f64(get_fixed(&lo_f[0][sl], &hi_f[0][sl]), f.se[0]);
-        if (twc) {
-          outX[g] = fixed_to_f64(get_fixed(&lo_f[1][sl], &hi_f[1][sl]), f.se[1]);
-          outY[g] = fixed_to_f64(get_fixed(&lo_f[2][sl], &hi_f[2][sl]), f.se[2]);
-          outZ[g] = fixed_to_f64(get_fixed(&lo_f[3][sl], &hi_f[3][sl]), f.se[3]);
+#pragma unroll
+      for (int fld = 0; fld < 5; ++fld) {
+        if (fld < 4 ? !DO_INT : !DO_NEW) continue;
+        const int q = fld < 4 ? fld : FE;
+        long long v;
+        if (tile) {
+          v = __ldcg(&tile[q * NB3 + s]);
+          tile[q * NB3 + s] = 0;  // ready for the next launch
         } else {
-          outX[g] = 0.0; outY[g] = 0.0; outZ[g] = 0.0;
+          v = get_fixed(&lo_f[q][sl], &hi_f[q][sl]);
         }
+        outs[fld][g] = (fld >= 1 && fld <= 3 && !twc) ? 0.0 : fixed_to_f64(v, f.se[fld]);
       }
-      if (DO_NEW) outE[g] = fixed_to_f64(get_fixed(&lo_f[FE][sl], &hi_f[FE][sl]), f.se[4]);
     }
+    if (tile && threadIdx.x == 0) w.done[slot] = 0;
     __syncthreads();
   }
 }
@@ -1287,10 +1283,11 @@ int sort_step(pstep_ctx *h) {
   {  // deposit work list for this step's particle distribution
     Work &w = f.work;
     const int nbk = w.nbd;
+    const int wblocks = (int)(((int64_t)nbk * 32 + kThreads - 1) / kThreads);  // one warp per brick
     if (w.br == 16)
-      k_work_count<16><<<nb(nbk), kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+      k_work_count<16><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
     else
-      k_work_count<8><<<nb(nbk), kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+      k_work_count<8><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
     PSTEP_LAUNCHED(h);
     TRY32(exclusive_scan(h, w.cnt_a, nbk, w.off_a, nullptr));
     TRY32(exclusive_scan(h, w.cnt_b, nbk, w.off_b, nullptr));
@@ -1344,11 +1341,15 @@ int f32_create(pstep_ctx *h) {
       if (G.n[d] % 16 != 0 || G.n[d] < 32) w.br = 8;
     const int64_t nbk = (int64_t)(G.n[0] / w.br) * (G.n[1] / w.br) * (G.n[2] / w.br);
     w.nbd = (int)nbk;
-    const int64_t split_min = w.br == 16 ? DepTraits<16>::kChunkVisits / DepTraits<16>::kVisitFactor
-                                         : DepTraits<8>::kChunkVisits / DepTraits<8>::kVisitFactor;
-    w.slot_cap = (int64_t)h->cap / split_min + 1;
+    // a split brick's window holds more than kChunkMax particles and the windows
+    // hold at most kVisit * cap particles in all
+    const int64_t visit = w.br == 16 ? DepTraits<16>::kVisit : DepTraits<8>::kVisit;
+    w.slot_cap = visit * (int64_t)h->cap / kChunkMax + 1;
+    w.err = h->err_word;
     const int64_t br3 = (int64_t)w.br * w.br * w.br;
-    TRY32(dalloc32(h, w.items, (size_t)(nbk + 2 * w.slot_cap * 2 + 64)));
+    // items: one per unsplit brick plus ceil(window / kChunkMax) <= 2 window / kChunkMax
+    // per split brick, so at most nbk + 2 * kVisit * cap / kChunkMax
+    TRY32(dalloc32(h, w.items, (size_t)(nbk + 2 * w.slot_cap + 64)));
     TRY32(dalloc32(h, w.nchunk, (size_t)nbk));
     TRY32(dalloc32(h, w.slot, (size_t)nbk));
     int32_t **scan_arrays[6] = {&w.cnt_a, &w.cnt_b, &w.cnt_s, &w.off_a, &w.off_b, &w.off_s};
@@ -1685,7 +1686,6 @@ int dep_run(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN, double *
 
 int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   F32Form &f = *h->f32;
-  const Geom &G = h->geom;
   k_scales<<<1, 32, 0, h->stream>>>(f);  // fold this advance's maxima into the fixed-point scales
   PSTEP_LAUNCHED(h);
   PSTEP_CUDA(cudaMemsetAsync(f.work.next, 0, sizeof(int32_t), h->stream));

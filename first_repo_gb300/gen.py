@@ -85,11 +85,11 @@ def loguniform(seed: int, stream: int, count: int, lo: float, hi: float) -> np.n
     return out
 
 
-def make_case(n: int, count: int, seed: int, clustered: bool, l: float = 2 * 3.141592653589793):
+def make_case(n: int, count: int, seed: int, clustered: bool, l: float = 2 * 3.141592653589793, nblobs: int = 64):
     """Fields (interior) and particles of one synthetic case: u_p = interpolated gas velocity, T_p = 1."""
     ux, uy, uz = velocity(n, seed)
     tf = temperature(n, seed + 7)
-    x, y, z = positions(n, l, seed + 13, count, clustered)
+    x, y, z = positions(n, l, seed + 13, count, clustered, nblobs=nblobs)
     u, v, w = interp_velocity(n, l, x, y, z, ux, uy, uz)
     t = np.ones(count)
     flag = np.arange(count, dtype=np.int32)

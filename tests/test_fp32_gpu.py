@@ -106,29 +106,36 @@ def test_fp32_rejects_unsupported_grid(built_cuda):
     assert e.value.status == 2
 
 
-def brick_max(x, y, z, n, L, br):
-    """most particles whose cell lies in one br^3 brick"""
-    idx = [np.floor(a / (L / n)).astype(np.int64) // br for a in (x, y, z)]
-    nb = n // br
-    return int(np.bincount((idx[2] * nb + idx[1]) * nb + idx[0]).max())
+def window_max(x, y, z, n, L, br):
+    """most particles in one deposit brick's source window (the br^3 brick and two
+    cells around it, periodic)"""
+    idx = [np.floor(a / (L / n)).astype(np.int64) for a in (x, y, z)]
+    cnt = np.bincount((idx[2] * n + idx[1]) * n + idx[0], minlength=n ** 3).reshape(n, n, n)
+    best = 0
+    for bz in range(0, n, br):
+        for by in range(0, n, br):
+            for bx in range(0, n, br):
+                r = [np.arange(b - 2, b + br + 2) % n for b in (bz, by, bx)]
+                best = max(best, int(cnt[np.ix_(*r)].sum()))
+    return best
 
 
-# deposit brick edge (16 where every side is a multiple of 16 and at least 32, else 8)
-# and the brick population above which the deposit splits a brick into slices
-SPLIT_AT = {8: 8192, 16: 65536}
+# the deposit splits a brick into slices of at most this many window particles
+CHUNK_MAX = 1 << 16
 
 
-@pytest.mark.parametrize("n,count,br", [(32, 300000, 16), (24, 60000, 8)])
+@pytest.mark.parametrize("n,count,br", [(32, 300000, 16), (24, 200000, 8)])
 def test_fp32_dense_blob_split_bricks(built_cuda, n, count, br):
-    """A single tight blob puts more particles into one deposit brick than one CTA
-    takes, so the deposit splits it into slices combined in global memory; still
-    within the bound and bit-identical across runs. Both brick edges."""
+    """A single tight blob puts more particles into one deposit brick's source window
+    than one work item takes, so the deposit splits the brick into slices combined in
+    global memory; still within the bound and bit-identical across runs. Both brick
+    edges (16 where every side is a multiple of 16 and at least 32, else 8)."""
     bp = helpers.make_bp(n, count)
     L = bp.l
     ux, uy, uz = gen.velocity(n, 41)
     tf = gen.temperature(n, 42)
     x, y, z = gen.positions(n, L, 43, count, True, nblobs=1, sigma_cells=1.5)
-    assert brick_max(x, y, z, n, L, br) > SPLIT_AT[br]
+    assert window_max(x, y, z, n, L, br) > CHUNK_MAX
     u, v, w = gen.interp_velocity(n, L, x, y, z, ux, uy, uz)
     t = np.ones(count)
     flag = np.arange(count, dtype=np.int32)
