@@ -104,7 +104,6 @@ struct F32Form {
   uint32_t *key;      // brick-major cell id of the base position
   int32_t *cell_start;  // n^3 + 1, brick-major order (per step)
   int32_t *sidx;
-  float *tmpf;        // permutation scratch
   uint32_t *bounds;   // [0..2] max |RHS_u| per component (float bits), [3] max |RHS_T|, [4] max per-cell count
   uint32_t *slots;    // kBoundSlots x 4 partial maxima (spread so blocks do not contend on one word)
   int32_t *se;        // fixed-point scale exponents per field
@@ -1159,10 +1158,26 @@ __global__ void k_keys32(Geom G, Set32 S, int64_t n, uint32_t *__restrict__ key)
   key[p] = brick_id(G, ci_(c), cj_(c), ck_(c));
 }
 
-template <typename T>
-__global__ void k_perm(const T *__restrict__ src, const int32_t *__restrict__ idx, int64_t n, T *__restrict__ dst) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = src[idx[i]];
+// Per-particle arrays gathered through the sort permutation, up to kPermBatch
+// arrays of one element type per launch: the permutation is read once per batch
+// and every thread keeps one independent load per array in flight (a gather of
+// one array per launch is bound by load latency, not bandwidth).
+constexpr int kPermBatch = 8;
+template <typename T> struct PermBatch {
+  const T *src[kPermBatch];
+  T *dst[kPermBatch];
+};
+template <typename T, int K>
+__global__ void __launch_bounds__(256) k_perm_batch(PermBatch<T> b, const int32_t *__restrict__ idx, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t j = __ldcs(idx + i);
+    T v[K];
+#pragma unroll
+    for (int a = 0; a < K; ++a) v[a] = __ldcs(b.src[a] + j);
+#pragma unroll
+    for (int a = 0; a < K; ++a) __stcs(b.dst[a] + i, v[a]);
+  }
 }
 
 __global__ void k_f32_to_f64(const float *__restrict__ src, int64_t n, double *__restrict__ dst) {
@@ -1247,35 +1262,62 @@ int sort_step(pstep_ctx *h) {
   TRY32(csr_sort(h, f.key, 0, ncell, h->s.flag, f.cell_start, f.sidx, 0));
   if (n > 0) {
     Set32 &B = f.set[SBASE];
-    auto permf = [&](float *&a) {
-      k_perm<float><<<nb(n), kThreads, 0, h->stream>>>(a, f.sidx, n, f.tmpf);
-      float *t = a; a = f.tmpf; f.tmpf = t;
-    };
-    for (int d = 0; d < 3; ++d) permf(B.o[d]);
-    for (int q = 0; q < 4; ++q) permf(B.v[q]);
-    permf(f.rhs_t);
-    if (f.itp) permf(f.itp);
+    // every 4-byte per-particle array that lives across steps; the addresses of their
+    // pointer fields (float *, uint32_t *, int32_t *), swapped through memcpy
+    void *arrs[32];
+    int na = 0;
+    for (int d = 0; d < 3; ++d) arrs[na++] = &B.o[d];
+    for (int q = 0; q < 4; ++q) arrs[na++] = &B.v[q];
+    arrs[na++] = &B.cell;
+    arrs[na++] = &h->s.flag;
+    arrs[na++] = &f.rhs_t;
+    if (f.itp) arrs[na++] = &f.itp;
     for (int q = 0; q < 7; ++q)
-      if (f.pp[q]) permf(f.pp[q]);
+      if (f.pp[q]) arrs[na++] = &f.pp[q];
     for (int q = 0; q < 4; ++q)
-      if (f.gas[q]) permf(f.gas[q]);
+      if (f.gas[q]) arrs[na++] = &f.gas[q];
     for (int q = 0; q < 4; ++q)
-      if (f.drive[q]) permf(f.drive[q]);
+      if (f.drive[q]) arrs[na++] = &f.drive[q];
+    // Scratch: the *_np1 set's 8 arrays. After the step's last stage the base set
+    // holds the new positions and every *_int, *_new and *_np1 query reads the base
+    // set, so the stage sets carry nothing across the step boundary.
+    Set32 &S = f.set[SNP1];
+    void *scr[kPermBatch] = {&S.cell, &S.o[0], &S.o[1], &S.o[2], &S.v[0], &S.v[1], &S.v[2], &S.v[3]};
+    auto get = [](void *field) { void *p; memcpy(&p, field, sizeof p); return p; };
+    auto put = [](void *field, void *p) { memcpy(field, &p, sizeof p); };
+    const int pgrid = h->num_sms * 8;
+    for (int a0 = 0; a0 < na; a0 += kPermBatch) {
+      const int k = na - a0 < kPermBatch ? na - a0 : kPermBatch;
+      PermBatch<uint32_t> pb{};
+      for (int a = 0; a < k; ++a) {
+        pb.src[a] = (const uint32_t *)get(arrs[a0 + a]);
+        pb.dst[a] = (uint32_t *)get(scr[a]);
+      }
+      switch (k) {
+        case 1: k_perm_batch<uint32_t, 1><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+        case 2: k_perm_batch<uint32_t, 2><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+        case 3: k_perm_batch<uint32_t, 3><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+        case 4: k_perm_batch<uint32_t, 4><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+        case 5: k_perm_batch<uint32_t, 5><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+        case 6: k_perm_batch<uint32_t, 6><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+        case 7: k_perm_batch<uint32_t, 7><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+        default: k_perm_batch<uint32_t, 8><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n); break;
+      }
+      PSTEP_LAUNCHED(h);
+      for (int a = 0; a < k; ++a) {  // the gathered copy takes the array's place; the old one is scratch
+        void *old = get(arrs[a0 + a]);
+        put(arrs[a0 + a], pb.dst[a]);
+        put(scr[a], old);
+      }
+    }
     if (f.corr_y) {
-      k_perm<uint2><<<nb(n), kThreads, 0, h->stream>>>(f.corr_y, f.sidx, n, f.corr_y_tmp);
+      PermBatch<uint2> pb{};
+      pb.src[0] = f.corr_y;
+      pb.dst[0] = f.corr_y_tmp;
+      k_perm_batch<uint2, 1><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n);
+      PSTEP_LAUNCHED(h);
       uint2 *t = f.corr_y; f.corr_y = f.corr_y_tmp; f.corr_y_tmp = t;
-      h->launches += 1;
     }
-    {
-      k_perm<uint32_t><<<nb(n), kThreads, 0, h->stream>>>(B.cell, f.sidx, n, (uint32_t *)f.tmpf);
-      uint32_t *t = B.cell; B.cell = (uint32_t *)f.tmpf; f.tmpf = (float *)t;
-    }
-    {
-      k_perm<int32_t><<<nb(n), kThreads, 0, h->stream>>>(h->s.flag, f.sidx, n, (int32_t *)f.tmpf);
-      int32_t *t = h->s.flag; h->s.flag = (int32_t *)f.tmpf; f.tmpf = (float *)t;
-    }
-    h->launches += 9;
-    PSTEP_LAUNCHED(h);
     PSTEP_CUDA(cudaMemsetAsync(&f.bounds[4], 0, sizeof(uint32_t), h->stream));
     k_max_count<<<1024, kThreads, 0, h->stream>>>(f.cell_start, ncell, &f.bounds[4]);
     PSTEP_LAUNCHED(h);
@@ -1333,7 +1375,6 @@ int f32_create(pstep_ctx *h) {
   const size_t ncell = (size_t)G.n[0] * G.n[1] * G.n[2];
   TRY32(dalloc32(h, f->cell_start, ncell + 1));
   TRY32(dalloc32(h, f->sidx, cap));
-  TRY32(dalloc32(h, f->tmpf, cap));
   {  // deposit work list
     Work &w = f->work;
     w.br = 16;
@@ -1386,7 +1427,7 @@ int f32_destroy(pstep_ctx *h) {
   for (int q = 0; q < 4; ++q) dfree32(f->drive[q]);
   dfree32(f->corr_y); dfree32(f->corr_y_tmp);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
-  dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx); dfree32(f->tmpf);
+  dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx);
   dfree32(f->bounds); dfree32(f->se); dfree32(f->slots);
   {
     Work &w = f->work;
