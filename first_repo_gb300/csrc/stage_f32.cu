@@ -404,13 +404,6 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 __device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
 
-// SiLU z * sigmoid(z) = z/2 * (1 + tanh(z/2)) with the hardware tanh approximation
-__device__ __forceinline__ float silu_fast(float z) {
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
-  return 0.5f * z * (1.f + t);
-}
-
 // warpgroup-local barrier (named barrier 1 + group, 128 threads; immediate ids)
 __device__ __forceinline__ void group_bar(int wg) {
   if (wg == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
@@ -447,6 +440,13 @@ __device__ __forceinline__ bool group_wait(int wg, uint64_t *mbar, uint32_t &pha
 }
 
 // 16 accumulator columns + bias -> SiLU -> bf16, into row r, columns [c0, c0+16) of a 64-column tile
+// SiLU z * sigmoid(z) = z/2 * (1 + tanh(z/2)) with the hardware tanh approximation
+__device__ __forceinline__ float silu_fast(float z) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+  return 0.5f * z * (1.f + t);
+}
+
 __device__ __forceinline__ void silu_chunk_to_tile(uint8_t *tile, int r, int c0, const float (&v)[16],
                                                    const float *bias) {
   float h[16];
@@ -953,8 +953,7 @@ template <int BR, int NF> struct DepSmem {
 // particles per stage: at the *_int positions the concentration and the face
 // momentum (DO_INT), at the *_new positions RHS_T (DO_NEW). Field slots:
 // 0 C, 1-3 RHS_RU x/y/z, 4 RHS_Part_Temp (scale exponents f.se[0..4]).
-// Each thread finds a particle's row segment by binary search over the
-// segments' prefix counts.
+// Each thread finds its particles' row segments from the segments' prefix counts.
 template <bool DO_INT, bool DO_NEW, int BR>
 __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w,
                                                                    int twc, double *__restrict__ outC,
@@ -1022,14 +1021,20 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     const int grp = (int)(threadIdx.x >> 5) + ((int)blockDim.x >> 5) * (int)((threadIdx.x >> 3) & 3);
     const int32_t g0 = t0 + (int32_t)(((int64_t)(t1 - t0) * grp) / ngroups);
     const int32_t g1 = t0 + (int32_t)(((int64_t)(t1 - t0) * (grp + 1)) / ngroups);
-    for (int32_t t = g0 + (int32_t)(threadIdx.x & 7); t < g1; t += 8) {
-      // segment: last r with pre[r] <= t
-      int lo = 0, hi = NR;
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (pre[mid] <= t) lo = mid; else hi = mid;
+    // segment of the thread's first particle: the last r with pre[r] <= t (binary
+    // search); later particles only move forward (pre[NR] = total > t ends the scan)
+    int seg = 0;
+    {
+      const int32_t tf = g0 + (int32_t)(threadIdx.x & 7);
+      int hi = NR;
+      while (hi - seg > 1) {
+        const int mid = (seg + hi) >> 1;
+        if (pre[mid] <= tf) seg = mid; else hi = mid;
       }
-      const int32_t p = beg[lo] + (t - pre[lo]);
+    }
+    for (int32_t t = g0 + (int32_t)(threadIdx.x & 7); t < g1; t += 8) {
+      while (pre[seg + 1] <= t) ++seg;
+      const int32_t p = beg[seg] + (t - pre[seg]);
       if (DO_INT) {
         const uint32_t c = SI.cell[p];
         int r3[3];
