@@ -440,18 +440,21 @@ __device__ __forceinline__ bool group_wait(int wg, uint64_t *mbar, uint32_t &pha
 }
 
 // 16 accumulator columns + bias -> SiLU -> bf16, into row r, columns [c0, c0+16) of a 64-column tile
-// SiLU z * sigmoid(z) = z/2 * (1 + tanh(z/2)) with the hardware tanh approximation
-__device__ __forceinline__ float silu_fast(float z) {
+// SiLU z * sigmoid(z) = u (1 + tanh u) = u tanh(u) + u with u = z/2 and the hardware
+// tanh approximation; with the halved bias hb, u = v/2 + hb is one fma
+__device__ __forceinline__ float silu_half(float v, float hb) {
+  const float u = fmaf(v, 0.5f, hb);
   float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
-  return 0.5f * z * (1.f + t);
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return fmaf(u, t, u);
 }
 
+// bias: the layer's bias halved
 __device__ __forceinline__ void silu_chunk_to_tile(uint8_t *tile, int r, int c0, const float (&v)[16],
                                                    const float *bias) {
   float h[16];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) h[q] = silu_fast(v[q] + bias[c0 + q]);
+  for (int q = 0; q < 16; ++q) h[q] = silu_half(v[q], bias[c0 + q]);
 #pragma unroll
   for (int half = 0; half < 2; ++half) {
     uint4 w;
@@ -500,7 +503,9 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
   uint64_t *mbar = reinterpret_cast<uint64_t *>(gbase + corr::G_BAR);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + corr::TSLOT);
   for (uint32_t q = tid; q < corr::kImage / 16; q += corr::kThreads) reinterpret_cast<uint4 *>(sm)[q] = cd.image[q];
-  for (int q = tid; q < corr::kHid + corr::kHid + corr::kOutP; q += corr::kThreads) b1[q] = cd.bias[q];
+  // hidden-layer biases halved for silu_half (exact: a power-of-two scale)
+  for (int q = tid; q < corr::kHid + corr::kHid + corr::kOutP; q += corr::kThreads)
+    b1[q] = q < 2 * corr::kHid ? 0.5f * cd.bias[q] : cd.bias[q];
   if (lt == 0) mbar_init(mbar, 1);
   if (warp == 0) tmem_alloc(tslot, 128);
   tc05::fence_smem_async();
