@@ -333,19 +333,24 @@ def main():
                 "launches": dom_cnt}
     phases = {p: {"ms_per_step": v[0] / args.steps, "launch_groups": v[1]} for p, v in prof.items()}
 
-    # end to end through the C ABI with host buffers (pinned)
+    # end to end through the C ABI with host buffers (pinned): a time-stepping loop
+    # through host memory -- each step uploads the particles and fields, primes, runs
+    # one step and reads back every particle array (ids included) and every deposited
+    # field; the particles read back are the next step's inputs, in the order returned
     e2e = None
     if not args.no_e2e:
-        hp = [pinned_like(a) for a in arrs]
+        hin = [pinned_like(a) for a in arrs]
+        hout = [pinned_like(a) for a in arrs]
         hf = [pinned_like(f) for f in fields]
-        out_p = [pinned_like(np.empty(n)) for _ in range(7)]
         out_f = [pinned_like(np.empty_like(fields[0])) for _ in range(5)]
-        names = ["x", "y", "z", "u", "v", "w", "T"]
+        names = ["x", "y", "z", "u", "v", "w", "T", "flag"]
         import ctypes as C
         L = pstep.lib()
+        bufs = [hin, hout]
 
         def one_step():
-            g.load(*hp)
+            src, dst = bufs
+            g.load(*src)
             if corr_model is not None:
                 g.set_correction(corr_model, nu_gas)
             g.bind_velocity(*hf[:3])
@@ -353,9 +358,10 @@ def main():
             g.prime()
             g.run(1)
             for i, nm in enumerate(names):
-                g._ok(L.pstep_get_particle_array(g.h, pstep.ARRAY_IDS[nm], out_p[i].ctypes.data, 0))
+                g._ok(L.pstep_get_particle_array(g.h, pstep.ARRAY_IDS[nm], dst[i].ctypes.data, 0))
             for i, fname in enumerate(pstep.FIELD_IDS):
                 g._ok(L.pstep_get_field(g.h, pstep.FIELD_IDS[fname], out_f[i].ctypes.data, 0))
+            bufs.reverse()
 
         one_step()
         barrier()
@@ -365,10 +371,11 @@ def main():
             one_step()
         barrier()
         e2e_s = (time.perf_counter() - t0) / ke
-        h2d = sum(a.nbytes for a in hp) + sum(f.nbytes for f in hf)
-        d2h = sum(a.nbytes for a in out_p) + sum(f.nbytes for f in out_f)
+        h2d = sum(a.nbytes for a in hin) + sum(f.nbytes for f in hf)
+        d2h = sum(a.nbytes for a in hout) + sum(f.nbytes for f in out_f)
         e2e = {"value": world * n / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3}
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+               "loop": "host time-stepping: each step's particles read back are the next step's inputs"}
         del C
 
     # the plain FP32 step and the FP64 drop-in on the same inputs, timed the same way

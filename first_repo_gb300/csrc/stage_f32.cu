@@ -113,7 +113,15 @@ struct F32Form {
   int sorted;
   int tref_set;
   double tref;        // temperature reference (see above)
+  // host transfers: two staging slots of kStageArrays x kStageChunk doubles, filled and
+  // drained on a copy stream of their own so that the copy of one chunk overlaps the
+  // conversion of the other (created at the first host upload or download)
+  double *stage[2];
+  cudaStream_t copy_stream;
+  cudaEvent_t ev_copied[2], ev_used[2];
 };
+constexpr int64_t kStageChunk = 1 << 22;  // particles per staged chunk
+constexpr int kStageArrays = 7;
 
 namespace {
 
@@ -1116,13 +1124,15 @@ __global__ void k_to_f32(const double *__restrict__ src, int64_t n, double shift
 }
 
 // upload: absolute fp64 positions -> cell + fp32 offset (the reference's trunc cell)
+// particles p0 .. p0 + n - 1 from fp64 arrays holding them from index 0
 __global__ void k_from_f64(Geom G, F32Form f, const double *__restrict__ x, const double *__restrict__ y,
                            const double *__restrict__ z, const double *__restrict__ u, const double *__restrict__ v,
-                           const double *__restrict__ w, const double *__restrict__ t, double tref, int64_t n,
-                           int32_t *__restrict__ err) {
-  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const double X[3] = {x[p], y[p], z[p]};
+                           const double *__restrict__ w, const double *__restrict__ t, double tref, int64_t p0,
+                           int64_t n, int32_t *__restrict__ err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t p = p0 + i;
+  const double X[3] = {x[i], y[i], z[i]};
   int c[3];
   float o[3];
 #pragma unroll
@@ -1140,24 +1150,27 @@ __global__ void k_from_f64(Geom G, F32Form f, const double *__restrict__ x, cons
   B.cell[p] = pack(c[0], c[1], c[2]);
 #pragma unroll
   for (int d = 0; d < 3; ++d) B.o[d][p] = o[d];
-  B.v[0][p] = (float)u[p];
-  B.v[1][p] = (float)v[p];
-  B.v[2][p] = (float)w[p];
-  B.v[3][p] = (float)(t[p] - tref);
+  B.v[0][p] = (float)u[i];
+  B.v[1][p] = (float)v[i];
+  B.v[2][p] = (float)w[i];
+  B.v[3][p] = (float)(t[i] - tref);
 }
 
 // download: one array of a set as fp64 (positions back to absolute coordinates)
-__global__ void k_to_f64_arr(Geom G, Set32 S, int comp, double tref, int64_t n, double *__restrict__ dst) {
-  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
+// particles p0 .. p0 + n - 1 into dst[0 .. n)
+__global__ void k_to_f64_arr(Geom G, Set32 S, int comp, double tref, int64_t p0, int64_t n,
+                             double *__restrict__ dst) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int64_t p = p0 + q;
   if (comp < 3) {
     const uint32_t c = S.cell[p];
     const int i = comp == 0 ? ci_(c) : (comp == 1 ? cj_(c) : ck_(c));
-    dst[p] = ((double)i + (double)S.o[comp][p]) * (G.l[comp] / G.n[comp]);
+    dst[q] = ((double)i + (double)S.o[comp][p]) * (G.l[comp] / G.n[comp]);
   } else if (comp < 6) {
-    dst[p] = (double)S.v[comp - 3][p];
+    dst[q] = (double)S.v[comp - 3][p];
   } else {
-    dst[p] = (double)S.v[3][p] + tref;
+    dst[q] = (double)S.v[3][p] + tref;
   }
 }
 
@@ -1445,8 +1458,30 @@ int f32_destroy(pstep_ctx *h) {
     dfree32(w.off_a); dfree32(w.off_b); dfree32(w.off_s); dfree32(w.n_items); dfree32(w.next); dfree32(w.done);
     dfree32(w.tiles);
   }
+  if (f->stage[0]) {
+    cudaStreamSynchronize(f->copy_stream);
+    for (int sl = 0; sl < 2; ++sl) {
+      dfree32(f->stage[sl]);
+      cudaEventDestroy(f->ev_copied[sl]);
+      cudaEventDestroy(f->ev_used[sl]);
+    }
+    cudaStreamDestroy(f->copy_stream);
+  }
   delete f;
   h->f32 = nullptr;
+  return PSTEP_OK;
+}
+
+// the host-transfer staging of the FP32 form (first use)
+static int stage_init(pstep_ctx *h) {
+  F32Form &f = *h->f32;
+  if (f.stage[0]) return PSTEP_OK;
+  for (int sl = 0; sl < 2; ++sl) TRY32(dalloc32(h, f.stage[sl], (size_t)(kStageArrays * kStageChunk)));
+  PSTEP_CUDA(cudaStreamCreateWithFlags(&f.copy_stream, cudaStreamNonBlocking));
+  for (int sl = 0; sl < 2; ++sl) {
+    PSTEP_CUDA(cudaEventCreateWithFlags(&f.ev_copied[sl], cudaEventDisableTiming));
+    PSTEP_CUDA(cudaEventCreateWithFlags(&f.ev_used[sl], cudaEventDisableTiming));
+  }
   return PSTEP_OK;
 }
 
@@ -1469,21 +1504,33 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
     f.tref_set = 1;
   }
   const double *src[7] = {x, y, z, u, v, w, t};
-  double *tmp[7] = {nullptr};
-  if (!on_device) {
-    for (int q = 0; q < 7; ++q) {
-      TRY32(dalloc32(h, tmp[q], (size_t)n));
-      PSTEP_CUDA(cudaMemcpyAsync(tmp[q], src[q], sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
-      src[q] = tmp[q];
-    }
+  if (on_device) {
+    k_from_f64<<<nb(n), kThreads, 0, h->stream>>>(h->geom, f, src[0], src[1], src[2], src[3], src[4], src[5],
+                                                  src[6], f.tref, 0, n, h->err_word);
+    PSTEP_LAUNCHED(h);
+    return PSTEP_OK;
   }
-  k_from_f64<<<nb(n), kThreads, 0, h->stream>>>(h->geom, f, src[0], src[1], src[2], src[3], src[4], src[5], src[6],
-                                                f.tref, n, h->err_word);
-  PSTEP_LAUNCHED(h);
-  if (!on_device) {
-    PSTEP_CUDA(cudaStreamSynchronize(h->stream));
-    for (int q = 0; q < 7; ++q) dfree32(tmp[q]);
+  // host arrays: chunks of kStageChunk particles copied into the two staging slots in
+  // turn on the copy stream, each converted on the handle's stream once it has landed
+  TRY32(stage_init(h));
+  for (int64_t c = 0, p0 = 0; p0 < n; ++c, p0 += kStageChunk) {
+    const int sl = (int)(c & 1);
+    const int64_t len = n - p0 < kStageChunk ? n - p0 : kStageChunk;
+    if (c >= 2) PSTEP_CUDA(cudaStreamWaitEvent(f.copy_stream, f.ev_used[sl], 0));  // slot's last conversion done
+    double *b = f.stage[sl];
+    for (int q = 0; q < 7; ++q)
+      PSTEP_CUDA(cudaMemcpyAsync(b + q * kStageChunk, src[q] + p0, sizeof(double) * len, cudaMemcpyHostToDevice,
+                                 f.copy_stream));
+    PSTEP_CUDA(cudaEventRecord(f.ev_copied[sl], f.copy_stream));
+    PSTEP_CUDA(cudaStreamWaitEvent(h->stream, f.ev_copied[sl], 0));
+    k_from_f64<<<nb(len), kThreads, 0, h->stream>>>(h->geom, f, b, b + kStageChunk, b + 2 * kStageChunk,
+                                                    b + 3 * kStageChunk, b + 4 * kStageChunk, b + 5 * kStageChunk,
+                                                    b + 6 * kStageChunk, f.tref, p0, len, h->err_word);
+    PSTEP_LAUNCHED(h);
+    PSTEP_CUDA(cudaEventRecord(f.ev_used[sl], h->stream));
   }
+  // the host arrays may be reused when this returns: every copy has been read
+  PSTEP_CUDA(cudaStreamSynchronize(f.copy_stream));
   return PSTEP_OK;
 }
 
@@ -1793,20 +1840,39 @@ int f32_get_array(pstep_ctx *h, int id, void *dst, int on_device) {
     snprintf(h->err, sizeof h->err, "gas values per particle need the PSTEP_KEEP_GAS flag");
     return PSTEP_ERR_CONFIG;
   }
-  double *tmp = nullptr;
-  TRY32(dalloc32(h, tmp, (size_t)n));
-  if (set >= 0) {
-    k_to_f64_arr<<<nb(n), kThreads, 0, h->stream>>>(h->geom, f.set[set], comp, f.tref, n, tmp);
-  } else if (id >= PSTEP_UG) {
-    k_to_f32_shift<<<nb(n), kThreads, 0, h->stream>>>(f.gas[id - PSTEP_UG], n, id == PSTEP_TG ? f.tref : 0.0, tmp);
-  } else {
-    k_f32_to_f64<<<nb(n), kThreads, 0, h->stream>>>(f.rhs_t, n, tmp);  // RHS_T
+  // particles p0 .. p0 + len - 1 as fp64 into out[0 .. len)
+  auto convert = [&](int64_t p0, int64_t len, double *out) {
+    if (set >= 0) {
+      k_to_f64_arr<<<nb(len), kThreads, 0, h->stream>>>(h->geom, f.set[set], comp, f.tref, p0, len, out);
+    } else if (id >= PSTEP_UG) {
+      k_to_f32_shift<<<nb(len), kThreads, 0, h->stream>>>(f.gas[id - PSTEP_UG] + p0, len,
+                                                          id == PSTEP_TG ? f.tref : 0.0, out);
+    } else {
+      k_f32_to_f64<<<nb(len), kThreads, 0, h->stream>>>(f.rhs_t + p0, len, out);  // RHS_T
+    }
+  };
+  if (on_device) {
+    convert(0, n, (double *)dst);
+    PSTEP_LAUNCHED(h);
+    PSTEP_CUDA(cudaStreamSynchronize(h->stream));  // complete on return, as for host destinations
+    return PSTEP_OK;
   }
-  PSTEP_LAUNCHED(h);
-  PSTEP_CUDA(cudaMemcpyAsync(dst, tmp, sizeof(double) * n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                             h->stream));
-  PSTEP_CUDA(cudaStreamSynchronize(h->stream));
-  dfree32(tmp);
+  // host destination: chunks converted into the staging slots in turn and copied out on
+  // the copy stream, the copy of one overlapping the conversion of the next
+  TRY32(stage_init(h));
+  double *out = (double *)dst;
+  for (int64_t c = 0, p0 = 0; p0 < n; ++c, p0 += kStageChunk) {
+    const int sl = (int)(c & 1);
+    const int64_t len = n - p0 < kStageChunk ? n - p0 : kStageChunk;
+    if (c >= 2) PSTEP_CUDA(cudaStreamWaitEvent(h->stream, f.ev_copied[sl], 0));  // slot's last copy done
+    convert(p0, len, f.stage[sl]);
+    PSTEP_LAUNCHED(h);
+    PSTEP_CUDA(cudaEventRecord(f.ev_used[sl], h->stream));
+    PSTEP_CUDA(cudaStreamWaitEvent(f.copy_stream, f.ev_used[sl], 0));
+    PSTEP_CUDA(cudaMemcpyAsync(out + p0, f.stage[sl], sizeof(double) * len, cudaMemcpyDeviceToHost, f.copy_stream));
+    PSTEP_CUDA(cudaEventRecord(f.ev_copied[sl], f.copy_stream));
+  }
+  PSTEP_CUDA(cudaStreamSynchronize(f.copy_stream));
   return PSTEP_OK;
 }
 
