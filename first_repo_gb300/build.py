@@ -33,6 +33,7 @@ CU_UNITS = {
     "mlp.cu": ["-fmad=true"],
     "gas.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
+    "stats_io.cu": ["-fmad=false"],
 }
 
 

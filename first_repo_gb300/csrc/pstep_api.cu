@@ -233,6 +233,7 @@ const char *pstep_status_string(int s) {
     case PSTEP_ERR_MOVE: return "particle moved more than one cell";
     case PSTEP_ERR_NOMEM: return "device memory exhausted";
     case PSTEP_ERR_TIMEOUT: return "device wait timed out";
+    case PSTEP_ERR_IO: return "snapshot file error";
     default: return "unknown status";
   }
 }
@@ -351,6 +352,8 @@ int pstep_upload_particles(pstep_handle h, int64_t n, const double *x, const dou
   h->new_is_zero = 1;  // the reference's *_new vectors are zero-filled until the first stage writes them
   h->csr_prev.identity = 0;
   if (h->cfg.flags & PSTEP_TRACK_ORDER) TRY(order_init(h));
+  // host arrays may be reused or freed when this returns: every copy from them has completed
+  if (!on_device) PSTEP_CUDA(cudaStreamSynchronize(h->stream));
   if (h->cfg.flags & PSTEP_CHECK_INPUTS && !on_device) {
     for (int64_t i = 0; i < n; ++i) {
       const double p[3] = {x[i], y[i], z[i]};

@@ -1827,6 +1827,29 @@ int f32_end_step(pstep_ctx *h) {
   return rc;
 }
 
+namespace {
+__global__ void k_positions32(Geom G, Set32 S, const int32_t *__restrict__ idx, int32_t n, double *__restrict__ xyz) {
+  const int32_t i = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= n) return;
+  const int32_t p = idx[i];
+  if (p < 0) return;
+  const uint32_t c = S.cell[p];
+  const int cc[3] = {ci_(c), cj_(c), ck_(c)};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) xyz[3 * i + d] = ((double)cc[d] + (double)S.o[d][p]) * (G.l[d] / G.n[d]);
+}
+}  // namespace
+
+// positions (as pstep_get_particle_array returns them) of the particles at storage
+// indices idx[0 .. n) (negative: skipped) into xyz (device, 3 per particle)
+int f32_positions(pstep_ctx *h, const int32_t *idx, int32_t n, double *xyz) {
+  F32Form &f = *h->f32;
+  if (n <= 0) return PSTEP_OK;
+  k_positions32<<<(n + kThreads - 1) / kThreads, kThreads, 0, h->stream>>>(h->geom, f.set[SBASE], idx, n, xyz);
+  PSTEP_LAUNCHED(h);
+  return PSTEP_OK;
+}
+
 int f32_get_array(pstep_ctx *h, int id, void *dst, int on_device) {
   F32Form &f = *h->f32;
   const int64_t n = h->np;

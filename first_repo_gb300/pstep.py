@@ -28,7 +28,8 @@ FIELD_IDS = {"C": 0, "RHS_RU_x": 1, "RHS_RU_y": 2, "RHS_RU_z": 3, "RHS_Part_Temp
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported configuration", 3: "capacity exceeded",
           4: "call out of sequence", 5: "CUDA error", 6: "non-finite value", 7: "position out of range",
-          8: "particle moved more than one cell", 9: "device memory exhausted", 10: "device wait timed out"}
+          8: "particle moved more than one cell", 9: "device memory exhausted", 10: "device wait timed out",
+          11: "snapshot file error"}
 
 
 class PstepError(RuntimeError):
@@ -107,6 +108,13 @@ def lib():
     L.pstep_launch_count.restype = C.c_int64
     L.pstep_profile.argtypes = [_H, C.c_int]
     L.pstep_profile_read.argtypes = [_H, _D, C.POINTER(C.c_int64), C.c_int]
+    L.pstep_np_tot.argtypes = [_H, C.POINTER(C.c_int64)]
+    L.pstep_max.argtypes = [_H, C.c_int, _D]
+    L.pstep_balance_index.argtypes = [_H, _D]
+    L.pstep_field_stats.argtypes = [_H, C.c_int, _D, _D, _D]
+    L.pstep_find_tags.argtypes = [_H, _VP, C.c_int32, _VP, _VP]
+    L.pstep_store_all.argtypes = [_H, C.c_char_p, C.c_int]
+    L.pstep_load_all.argtypes = [_H, C.c_char_p, C.c_int64, C.c_int]
     L._typed = True
     return L
 
@@ -308,3 +316,40 @@ class ParticleStep:
 
     def launches(self) -> int:
         return int(self.L.pstep_launch_count(self.h))
+
+    # ---- diagnostics (particle.cpp:662-741, tensor0.cpp:418-503) ----
+    def np_tot(self) -> int:
+        v = C.c_int64()
+        self._ok(self.L.pstep_np_tot(self.h, C.byref(v)))
+        return v.value
+
+    def max(self, name: str) -> float:
+        v = C.c_double()
+        self._ok(self.L.pstep_max(self.h, ARRAY_IDS[name], C.byref(v)))
+        return v.value
+
+    def balance_index(self) -> float:
+        v = C.c_double()
+        self._ok(self.L.pstep_balance_index(self.h, C.byref(v)))
+        return v.value
+
+    def field_stats(self, name: str) -> tuple[float, float, float]:
+        """(max, min, mean) of a deposited field over the interior"""
+        mx, mn, me = C.c_double(), C.c_double(), C.c_double()
+        self._ok(self.L.pstep_field_stats(self.h, FIELD_IDS[name], C.byref(mx), C.byref(mn), C.byref(me)))
+        return mx.value, mn.value, me.value
+
+    def find_tags(self, tags) -> tuple[np.ndarray, np.ndarray]:
+        """positions (n, 3) of the particles with the given ids, and found flags"""
+        t = np.ascontiguousarray(tags, dtype=np.int32)
+        xyz = np.zeros((t.size, 3))
+        found = np.zeros(t.size, dtype=np.int32)
+        self._ok(self.L.pstep_find_tags(self.h, t.ctypes.data, t.size, xyz.ctypes.data, found.ctypes.data))
+        return xyz, found.astype(bool)
+
+    # ---- snapshot files (particle.cpp:867-1025) ----
+    def store_all(self, data_dir: str, num_ts: int):
+        self._ok(self.L.pstep_store_all(self.h, data_dir.encode(), int(num_ts)))
+
+    def load_all(self, directory: str, n0: int, box: bool = True):
+        self._ok(self.L.pstep_load_all(self.h, directory.encode(), int(n0), 1 if box else 0))

@@ -53,7 +53,8 @@ typedef enum {
                                reference indexes past its ghost layer) */
   PSTEP_ERR_MOVE = 8,       /* a particle moved more than one cell in one stage */
   PSTEP_ERR_NOMEM = 9,      /* device allocation failed */
-  PSTEP_ERR_TIMEOUT = 10    /* a bounded device-side wait gave up */
+  PSTEP_ERR_TIMEOUT = 10,   /* a bounded device-side wait gave up */
+  PSTEP_ERR_IO = 11         /* a snapshot file could not be created, read or written */
 } pstep_status;
 
 enum { PSTEP_FP64 = 0, PSTEP_FP32 = 1 };
@@ -267,6 +268,42 @@ int pstep_profile_read(pstep_handle h, double *ms, int64_t *counts, int nphases)
 int pstep_last_run_ms(pstep_handle h, double *ms);
 /* Number of kernel launches enqueued by this handle since creation. */
 int64_t pstep_launch_count(pstep_handle h);
+
+/* ---- Diagnostics: the reference's particle statistics and the extrema of the
+ * deposited fields that its statistics output takes (grid.cpp:715-735). All
+ * synchronise the stream; results are for this handle (one rank). ---- */
+/* particle::NP_TOT (particle.cpp:662-669): the particle count (summed over ranks) */
+int pstep_np_tot(pstep_handle h, int64_t *out);
+/* particle::max (particle.cpp:671-685) of one particle array (PSTEP_X ... PSTEP_TG, not
+ * PSTEP_FLAG), as pstep_get_particle_array would return it: its largest value, or -1e9
+ * when there are no particles */
+int pstep_max(pstep_handle h, int id, double *out);
+/* particle::Balance_Index (particle.cpp:730-741): largest over smallest per-rank particle
+ * count; one rank: Np / Np (NaN when there are no particles) */
+int pstep_balance_index(pstep_handle h, double *out);
+/* tensor0::max, ::min and ::mean (tensor0.cpp:452-463, 492-503, 418-435) of a deposited
+ * field (PSTEP_FIELD_*), over the interior cells. The maximum and minimum are exact; the
+ * mean is the interior sum (taken in a fixed order, not the reference's i-j-k loop
+ * order, so it can differ in the last bits) over n^3. Any of the outputs may be NULL. */
+int pstep_field_stats(pstep_handle h, int field, double *max, double *min, double *mean);
+/* particle::find_tag (particle.cpp:721-731) for n ids: xyz[3 i .. 3 i + 2] = the position of
+ * the particle with id tags[i] and found[i] = 1, or found[i] = 0 (xyz untouched) when no
+ * particle has it. particle::trajectory (:687-719) asks it for ids 0, K, 2K, ... */
+int pstep_find_tags(pstep_handle h, const int32_t *tags, int32_t n, double *xyz, int32_t *found);
+
+/* ---- Snapshot files: particle::Store_All / Load_All (particle.cpp:867-1025), one rank.
+ * Raw native-endian arrays, one file per quantity: doubles for x y z u v w T, int32 for
+ * the ids. ---- */
+/* writes <data_dir>Part_{x,y,z,u,v,w,T,flag}_<num_ts>.bin (data_dir is a prefix, as
+ * params.data_dir(); include the trailing '/'), in the order pstep_get_particle_array
+ * returns (with PSTEP_TRACK_ORDER: the reference's order, byte-identical to its files).
+ * A file that exists already is an error (MPI_MODE_EXCL), PSTEP_ERR_IO. */
+int pstep_store_all(pstep_handle h, const char *data_dir, int num_ts);
+/* reads n0 particles from <dir>Restart_Part_{x,...,flag}.bin (box != 0) or
+ * <dir>Restart_Part_{x,...,flag}_IO.bin (the IO duct's files) and uploads them as
+ * pstep_upload_particles does; a missing or short file is PSTEP_ERR_IO. The reference
+ * then runs Send_Recv, which on one rank changes nothing for positions inside the box. */
+int pstep_load_all(pstep_handle h, const char *dir, int64_t n0, int box);
 
 #ifdef __cplusplus
 }

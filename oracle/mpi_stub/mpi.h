@@ -14,7 +14,9 @@
  *    with the same tag. The reference posts Irecv before it fills the send
  *    buffer (particle.cpp:751-755), so matching happens at Waitall time.
  *  - reductions, broadcasts, gathers and scatters are copies.
- *  - MPI-IO is not used by the harness; calling it aborts.
+ *  - MPI-IO is plain stdio on the one file: open (MPI_MODE_EXCL refuses an existing
+ *    file), read/write at a byte offset, close; the views and collectives reduce to
+ *    that on one rank.
  */
 #ifndef PSTEP_ORACLE_MPI_STUB_H
 #define PSTEP_ORACLE_MPI_STUB_H
@@ -31,7 +33,7 @@ typedef int MPI_Info;
 typedef int MPI_Request;
 typedef long long MPI_Offset;
 typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
-typedef struct { int dummy; } *MPI_File;
+typedef FILE *MPI_File;
 
 #define MPI_SUCCESS 0
 #define MPI_COMM_WORLD 1
@@ -154,13 +156,29 @@ static inline int MPI_Scatter(const void *s, int n, MPI_Datatype t, void *r, int
   memmove(r, s, (size_t)n * mpistub_size(t)); return 0;
 }
 
-static inline int MPI_File_open(MPI_Comm, const char *, int, MPI_Info, MPI_File *) { mpistub_fail("MPI-IO not supported"); return 1; }
-static inline int MPI_File_close(MPI_File *) { mpistub_fail("MPI-IO not supported"); return 1; }
-static inline int MPI_File_set_view(MPI_File, MPI_Offset, MPI_Datatype, MPI_Datatype, const char *, MPI_Info) { mpistub_fail("MPI-IO"); return 1; }
-static inline int MPI_File_read_all(MPI_File, void *, int, MPI_Datatype, MPI_Status *) { mpistub_fail("MPI-IO"); return 1; }
-static inline int MPI_File_write_all(MPI_File, const void *, int, MPI_Datatype, MPI_Status *) { mpistub_fail("MPI-IO"); return 1; }
-static inline int MPI_File_read_at_all(MPI_File, MPI_Offset, void *, int, MPI_Datatype, MPI_Status *) { mpistub_fail("MPI-IO"); return 1; }
-static inline int MPI_File_write_at_all(MPI_File, MPI_Offset, const void *, int, MPI_Datatype, MPI_Status *) { mpistub_fail("MPI-IO"); return 1; }
+static inline int MPI_File_open(MPI_Comm, const char *name, int amode, MPI_Info, MPI_File *fh) {
+  const char *mode = (amode & MPI_MODE_RDONLY) ? "rb" : ((amode & MPI_MODE_EXCL) ? "wbx" : "wb");
+  *fh = fopen(name, mode);
+  return *fh ? MPI_SUCCESS : 1;
+}
+static inline int MPI_File_close(MPI_File *fh) {
+  if (*fh) fclose(*fh);
+  *fh = NULL;
+  return MPI_SUCCESS;
+}
+static inline int MPI_File_set_view(MPI_File, MPI_Offset, MPI_Datatype, MPI_Datatype, const char *, MPI_Info) { mpistub_fail("MPI-IO views"); return 1; }
+static inline int MPI_File_read_all(MPI_File, void *, int, MPI_Datatype, MPI_Status *) { mpistub_fail("MPI-IO read_all"); return 1; }
+static inline int MPI_File_write_all(MPI_File, const void *, int, MPI_Datatype, MPI_Status *) { mpistub_fail("MPI-IO write_all"); return 1; }
+static inline int MPI_File_read_at_all(MPI_File fh, MPI_Offset off, void *buf, int n, MPI_Datatype t, MPI_Status *) {
+  if (!fh) mpistub_fail("read from a file that did not open");
+  if (fseek(fh, (long)off, SEEK_SET) != 0) return 1;
+  return fread(buf, mpistub_size(t), (size_t)n, fh) == (size_t)n ? MPI_SUCCESS : 1;
+}
+static inline int MPI_File_write_at_all(MPI_File fh, MPI_Offset off, const void *buf, int n, MPI_Datatype t, MPI_Status *) {
+  if (!fh) mpistub_fail("write to a file that did not open");
+  if (fseek(fh, (long)off, SEEK_SET) != 0) return 1;
+  return fwrite(buf, mpistub_size(t), (size_t)n, fh) == (size_t)n ? MPI_SUCCESS : 1;
+}
 static inline int MPI_File_get_size(MPI_File, MPI_Offset *) { mpistub_fail("MPI-IO"); return 1; }
 
 #ifdef __cplusplus

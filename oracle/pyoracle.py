@@ -3,9 +3,13 @@ __graft_entry__.smoke() and bench.py's CPU-baseline leg.
 
   Oracle      ctypes wrapper of oracle/_build/libpstep_oracle.so (the C restatement)
   run_ref     runs oracle/_ref/ref_harness (the reference's own sources, built here)
+  store_all, load_all, stats restatements   the snapshot files and statistics
+              (particle.cpp:662-741, 867-1025; tensor0.cpp:418-503)
+  run_ref_snapshot   the harness's Store_All / Load_All / statistics mode
 """
 from __future__ import annotations
 
+import json
 import ctypes as C
 import os
 import subprocess
@@ -213,6 +217,94 @@ def read_records(path: str, n_cells: int) -> list[dict]:
         off += 8
         recs.append(rec)
     return recs
+
+
+# ---------------------------------------------------------------- snapshots and statistics
+SNAP_NAMES = ["Part_x", "Part_y", "Part_z", "Part_u", "Part_v", "Part_w", "Part_T", "Part_flag"]
+SNAP_KEYS = ["x", "y", "z", "u", "v", "w", "T", "flag"]
+
+
+def store_all(data_dir: str, num_ts: int, arrays: dict) -> None:
+    """particle::Store_All on one rank (particle.cpp:867-919): each quantity as raw
+    native-endian values (double; int32 for the ids) in <data_dir><name>_<num_ts>.bin,
+    offset 0, refusing an existing file (MPI_MODE_EXCL)."""
+    for name, key in zip(SNAP_NAMES, SNAP_KEYS):
+        dt = np.int32 if key == "flag" else np.float64
+        with open(f"{data_dir}{name}_{num_ts}.bin", "xb") as f:
+            f.write(np.ascontiguousarray(arrays[key], dtype=dt).tobytes())
+
+
+def load_all(directory: str, n0: int, box: bool = True) -> dict:
+    """particle::Load_All on one rank (particle.cpp:948-1025): n0 values of each
+    quantity from <dir>Restart_<name>.bin (the IO duct's files with _IO)."""
+    out = {}
+    for name, key in zip(SNAP_NAMES, SNAP_KEYS):
+        dt = np.int32 if key == "flag" else np.float64
+        a = np.fromfile(f"{directory}Restart_{name}{'' if box else '_IO'}.bin", dtype=dt, count=n0)
+        if a.size != n0:
+            raise IOError(f"short restart file for {name}")
+        out[key] = a
+    return out
+
+
+def array_max(v: np.ndarray) -> float:
+    """particle::max (particle.cpp:671-685): -1e9 without particles, else the first
+    element raised by every strictly larger one"""
+    if v.size == 0:
+        return -1e9
+    m = v[0]
+    larger = v[v > m]
+    return float(max(m, larger.max())) if larger.size else float(m)
+
+
+def field_stats(f: np.ndarray, n: int) -> tuple[float, float, float]:
+    """tensor0::max, ::min (tensor0.cpp:452-463, 492-503) over the interior and ::mean
+    (:418-435): the interior sum in the reference's i-j-k loop order over size_tot"""
+    interior = f[1:n + 1, 1:n + 1, 1:n + 1]  # [k][j][i]
+    s = 0.0
+    for v in np.ascontiguousarray(interior.transpose(2, 1, 0)).ravel():  # i outermost, k innermost
+        s += float(v)
+    return float(interior.max()), float(interior.min()), s / float(n * n * n)
+
+
+def trajectory_ids(n0: int, np_track: int) -> list[int]:
+    """ids particle::trajectory reports (particle.cpp:687-719): 0, K, 2K, ... < N0,
+    K = ceil(N0 / Np_track)"""
+    if np_track == 0:
+        return []
+    k = (n0 + np_track - 1) // np_track
+    return list(range(0, n0, k))
+
+
+def run_ref_snapshot(bp, case: dict, nsteps: int, workdir: str, store_ts: int = -1, load: bool = False,
+                     np_track: int = 0) -> tuple[list[dict], dict | None, list[list[float]]]:
+    """Run the harness with Store_All (store_ts >= 0), statistics and trajectory
+    (np_track > 0, statistics on) and/or Load_All (load: Restart_Part_*.bin in workdir).
+    Returns the records, the STATS line and the trajectory rows (time, then x y z per id)."""
+    if not os.path.exists(REF_BIN):
+        if build_ref() is None:
+            raise RuntimeError("reference sources are not available here")
+    pfile, ifile = write_case(workdir, bp, case)
+    if np_track:
+        lines = open(pfile).read().split("\n")
+        lines[4] = str(np_track)  # Np_track
+        lines[6] = "1 0"          # Statistics Stat_print
+        with open(pfile, "w") as f:
+            f.write("\n".join(lines))
+    ofile = os.path.join(workdir, "output.bin")
+    r = subprocess.run([REF_BIN, pfile, ifile, ofile, str(nsteps), "0", "0", str(store_ts), "1" if load else "0"],
+                       capture_output=True, text=True, cwd=workdir)
+    if r.returncode != 0:
+        raise RuntimeError("ref_harness failed:\n" + r.stdout + r.stderr)
+    stats = None
+    for line in r.stdout.splitlines():
+        if line.startswith("STATS "):
+            stats = json.loads(line[6:])
+    traj = []
+    tpath = os.path.join(workdir, "Part_trajectory.dat")
+    if os.path.exists(tpath):
+        traj = [[float(v) for v in ln.split()] for ln in open(tpath) if ln.strip()]
+    return read_records(ofile, bp.n), stats, traj
 
 
 def run_ref(bp, case: dict, nsteps: int, dump_all: bool = True, timing: bool = False, workdir: str | None = None):

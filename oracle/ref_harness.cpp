@@ -19,7 +19,17 @@
 // The fields are held fixed: U and T are given directly (the caller's
 // Equal_Divide forming, grid.cpp:662 and :676, is outside the step).
 //
-// usage: ref_harness params.in input.bin output.bin nsteps dump_all [time]
+// Optional, for the snapshot files and the statistics (particle.cpp:662-741, 867-1025):
+//   load     1: the particles come from the reference's Load_All (Restart_Part_*.bin in
+//            the working directory, N0 from params) instead of input.bin
+//   store_ts >= 0: after the run, Store_All(store_ts) (Part_*_<store_ts>.bin under the
+//            params data directory), trajectory(nsteps) when params track particles
+//            (Part_trajectory.dat under the statistics directory: the positions of ids
+//            0, K, 2K, ... through find_tag) and one line "STATS {json}" on stdout:
+//            NP_TOT, Balance_Index, max of x y z u v w T, C and RHS_Part_Temp
+//            max/min/mean
+//
+// usage: ref_harness params.in input.bin output.bin nsteps dump_all [time [store_ts [load]]]
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -86,6 +96,8 @@ int main(int argc, char **argv) {
   const int nsteps = atoi(argv[4]);
   const int dump_all = atoi(argv[5]);
   const int timing = argc > 6 ? atoi(argv[6]) : 0;
+  const int store_ts = argc > 7 ? atoi(argv[7]) : -1;
+  const int load = argc > 8 ? atoi(argv[8]) : 0;
   MPI_Init(&argc, &argv);
   params P(argv[1]);
   proc PC;
@@ -102,7 +114,7 @@ int main(int argc, char **argv) {
   read_exact(in, &np64, sizeof np64);
   read_exact(in, &nn, sizeof nn);
   if (nn != N) die("input grid size does not match params");
-  const int n = (int)np64;
+  int n = (int)np64;
   const size_t N3 = (size_t)N * N * N;
   std::vector<double> buf(N3);
 
@@ -118,15 +130,21 @@ int main(int argc, char **argv) {
   C = 0.; RHS_RU = 0.; RHS_Part_Temp = 0.;
 
   particle part(&P, &PC, &S);
-  part.Np = n;
-  std::vector<double> *dst[7] = {&part.x, &part.y, &part.z, &part.u, &part.v, &part.w, &part.T};
-  for (int a = 0; a < 7; ++a) {
-    dst[a]->resize(n);
-    read_exact(in, dst[a]->data(), (size_t)n * 8);
+  if (load) {
+    fclose(in);
+    part.Load_All();  // particle.cpp:948-985
+    n = part.Np;
+  } else {
+    part.Np = n;
+    std::vector<double> *dst[7] = {&part.x, &part.y, &part.z, &part.u, &part.v, &part.w, &part.T};
+    for (int a = 0; a < 7; ++a) {
+      dst[a]->resize(n);
+      read_exact(in, dst[a]->data(), (size_t)n * 8);
+    }
+    part.flag.resize(n);
+    read_exact(in, part.flag.data(), (size_t)n * 4);
+    fclose(in);
   }
-  part.flag.resize(n);
-  read_exact(in, part.flag.data(), (size_t)n * 4);
-  fclose(in);
   // RESIZE() (particle.cpp:136-148) reserves wg and Tg instead of resizing them;
   // size every work vector here so the reference's writes stay in bounds.
   std::vector<double> *work[] = {&part.x_int, &part.y_int, &part.z_int, &part.x_new, &part.y_new, &part.z_new,
@@ -183,6 +201,17 @@ int main(int argc, char **argv) {
   }
   dump(out, 1000000 + nsteps, part, C, RHS_RU, RHS_Part_Temp, N);
   fclose(out);
+  if (store_ts >= 0) {
+    part.Store_All(store_ts);
+    printf("STATS {\"np_tot\": %d, \"balance_index\": %.17g, \"max\": {", part.NP_TOT(), part.Balance_Index());
+    const char *nm[7] = {"x", "y", "z", "u", "v", "w", "T"};
+    std::vector<double> *arr[7] = {&part.x, &part.y, &part.z, &part.u, &part.v, &part.w, &part.T};
+    for (int a = 0; a < 7; ++a) printf("%s\"%s\": %.17g", a ? ", " : "", nm[a], part.max(*arr[a]));
+    printf("}, \"C\": [%.17g, %.17g, %.17g]", C.max(), C.min(), C.mean());
+    printf(", \"RHS_Part_Temp\": [%.17g, %.17g, %.17g]}\n", RHS_Part_Temp.max(), RHS_Part_Temp.min(),
+           RHS_Part_Temp.mean());
+    if (P.Np_track() > 0) part.trajectory((double)nsteps);
+  }
   MPI_Finalize();
   return 0;
 }
