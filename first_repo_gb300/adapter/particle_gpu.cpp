@@ -6,9 +6,12 @@
 // synchronised lazily:
 //  - host -> device once, at the first gas2part_Temp_int (grid::Initialize
 //    fills x, u, T, flag and copies *_int / *_np1 just before, grid.cpp:207-226);
-//  - device -> host when the reference reads them: max(), Store_All(),
-//    trajectory(). The interpolation work arrays ug, vg, wg, Tg and RHS_u/v/w
-//    are internal to the device step and are not synchronised.
+//  - device -> host when the reference reads them element by element. The
+//    statistics (NP_TOT, max, Balance_Index, trajectory) and Store_All run on
+//    the device state directly (pstep_np_tot, pstep_max, pstep_balance_index,
+//    pstep_find_tags, pstep_store_all) without a download. The interpolation
+//    work arrays ug, vg, wg, Tg and RHS_u/v/w are internal to the device step
+//    and are not synchronised.
 // grid::TimeAdvance_RK4 and grid::TimeAdvance copy the public vectors
 // (grid.cpp:705-712, 315-325); on the device these copies happen when the next
 // stage starts (the next gas2part_velocity), inferred from the stage index.
@@ -254,24 +257,62 @@ void particle::part2gas_Temp_new(tensor0 &A) {
   g.host_stale = 1;
 }
 
-// ---- statistics and storage (host side, after a download) ----
+// ---- statistics and storage ----
+// particle.cpp:662-669
 int particle::NP_TOT() {
   GpuState &g = state(this);
-  return g.uploaded ? (int)pstep_num_particles(g.h) : Np;
+  if (!g.uploaded) return Np;
+  int64_t n = 0;
+  check(g.h, pstep_np_tot(g.h, &n), "np_tot");
+  return (int)n;
 }
 
+// the device array a public vector of the reference stands for, or -1
+static int array_id(const particle *q, const std::vector<double> *v) {
+  const std::vector<double> *m[] = {&q->x, &q->y, &q->z, &q->u, &q->v, &q->w, &q->T};
+  for (int i = 0; i < 7; ++i)
+    if (m[i] == v) return PSTEP_X + i;
+  if (v == &q->RHS_T) return PSTEP_RHS_T;
+  if (v == &q->ug) return PSTEP_UG;
+  if (v == &q->vg) return PSTEP_VG;
+  if (v == &q->wg) return PSTEP_WG;
+  if (v == &q->Tg) return PSTEP_TG;
+  return -1;
+}
+
+// particle.cpp:671-685: on the device when the vector is one the device keeps
 double particle::max(std::vector<double> &V) {
+  GpuState &g = state(this);
+  const int id = array_id(this, &V);
+  double m = 0;
+  if (g.uploaded && id >= 0 && pstep_max(g.h, id, &m) == PSTEP_OK) return m;
   pull(this);
   if (Np == 0) return -1e9;
-  double m = V[0];
+  m = V[0];
   for (int i = 1; i < Np; ++i)
     if (V[i] > m) m = V[i];
   return m;
 }
 
-double particle::Balance_Index() { return 1.0; }
+// particle.cpp:730-741
+double particle::Balance_Index() {
+  GpuState &g = state(this);
+  if (!g.uploaded) return (double)Np / (double)Np;
+  double b = 0;
+  check(g.h, pstep_balance_index(g.h, &b), "balance_index");
+  return b;
+}
 
 bool particle::find_tag(int tag, double &xx, double &yy, double &zz) {
+  GpuState &g = state(this);
+  if (g.uploaded) {
+    double xyz[3];
+    int32_t found = 0;
+    const int32_t t = tag;
+    check(g.h, pstep_find_tags(g.h, &t, 1, xyz, &found), "find_tag");
+    if (found) { xx = xyz[0]; yy = xyz[1]; zz = xyz[2]; }
+    return found != 0;
+  }
   for (int i = 0; i < Np; ++i)
     if (flag[i] == tag) {
       xx = x[i];
@@ -282,23 +323,35 @@ bool particle::find_tag(int tag, double &xx, double &yy, double &zz) {
   return false;
 }
 
+// particle.cpp:687-719 for one rank: every tracked id located in one device pass
 void particle::trajectory(double t) {
   if (param_->Np_track() == 0) return;
-  pull(this);
   const int K = (param_->N0() + param_->Np_track() - 1) / param_->Np_track();
-  stat_trajectory << t << " ";
-  for (int i = 0; i < param_->N0(); i += K) {
-    double a = 0, b = 0, c = 0;
-    if (find_tag(i, a, b, c)) stat_trajectory << a << " " << b << " " << c << " ";
+  std::vector<int32_t> ids;
+  for (int i = 0; i < param_->N0(); i += K) ids.push_back(i);
+  std::vector<double> xyz(3 * ids.size());
+  std::vector<int32_t> found(ids.size(), 0);
+  GpuState &g = state(this);
+  if (g.uploaded) {
+    check(g.h, pstep_find_tags(g.h, ids.data(), (int32_t)ids.size(), xyz.data(), found.data()), "trajectory");
+  } else {
+    for (size_t q = 0; q < ids.size(); ++q)
+      found[q] = find_tag(ids[q], xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2]);
   }
+  stat_trajectory << t << " ";
+  for (size_t q = 0; q < ids.size(); ++q)
+    if (found[q]) stat_trajectory << xyz[3 * q] << " " << xyz[3 * q + 1] << " " << xyz[3 * q + 2] << " ";
   stat_trajectory << std::endl;
 }
 
 void particle::Store(char *name, int num_ts, double *p) {
   std::ostringstream fn;
   fn << param_->data_dir() << name << "_" << num_ts << ".bin";
-  FILE *f = fopen(fn.str().c_str(), "wb");
-  if (!f) return;
+  FILE *f = fopen(fn.str().c_str(), "wbx");  // MPI_MODE_EXCL
+  if (!f) {
+    std::cerr << "pstep: cannot create " << fn.str() << " (Store_All never overwrites a file)" << std::endl;
+    std::abort();
+  }
   fwrite(p, sizeof(double), (size_t)Np, f);
   fclose(f);
 }
@@ -306,14 +359,22 @@ void particle::Store(char *name, int num_ts, double *p) {
 void particle::Store(char *name, int num_ts, int *p) {
   std::ostringstream fn;
   fn << param_->data_dir() << name << "_" << num_ts << ".bin";
-  FILE *f = fopen(fn.str().c_str(), "wb");
-  if (!f) return;
+  FILE *f = fopen(fn.str().c_str(), "wbx");  // MPI_MODE_EXCL
+  if (!f) {
+    std::cerr << "pstep: cannot create " << fn.str() << " (Store_All never overwrites a file)" << std::endl;
+    std::abort();
+  }
   fwrite(p, sizeof(int), (size_t)Np, f);
   fclose(f);
 }
 
+// particle.cpp:867-890: straight from the device state once it lives there
 void particle::Store_All(int num_ts) {
-  pull(this);
+  GpuState &g = state(this);
+  if (g.uploaded) {
+    check(g.h, pstep_store_all(g.h, param_->data_dir().c_str(), num_ts), "store_all");
+    return;
+  }
   Store((char *)"Part_x", num_ts, x.data());
   Store((char *)"Part_y", num_ts, y.data());
   Store((char *)"Part_z", num_ts, z.data());
