@@ -784,11 +784,11 @@ __device__ inline int rel_local(int c, int b, int n) {
 // most kChunkMax = 2^16 particles. The sum is hi * 2^16 + lo, exact whatever the
 // order of the adds.
 constexpr int32_t kChunkMax = 1 << 16;
-__device__ __forceinline__ void add_fixed32(uint32_t *lo, uint32_t *hi, int32_t v, bool pred) {
-  if (pred) {
-    atomicAdd(lo, (uint32_t)v & 0xffffu);
-    atomicAdd(hi, (uint32_t)(v >> 16));
-  }
+// Contributions outside the brick (pred false) go to the lane's own sink words
+// (never read), so the adds are branch-free.
+__device__ __forceinline__ void add_fixed32(uint32_t *lo, uint32_t *hi, int32_t v, bool pred, uint32_t *sink) {
+  atomicAdd(pred ? lo : sink, (uint32_t)v & 0xffffu);
+  atomicAdd(pred ? hi : sink + 32, (uint32_t)(v >> 16));
 }
 __device__ __forceinline__ long long get_fixed(const uint32_t *lo, const uint32_t *hi) {
   return (long long)(int32_t)*hi * 65536ll + (long long)*lo;
@@ -875,7 +875,7 @@ __global__ void k_work_fill(Work w, int nb) {
 // node = cell + h, the 8 cells node - 1 .. node get products of x_l / (1 - x_l)
 template <int BR>
 __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, const int r3[3], const float o3[3],
-                                                  float val) {
+                                                  float val, uint32_t *sink) {
   float w[3][2];
   int t0[3];
   bool ok[3][2];
@@ -899,7 +899,7 @@ __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, co
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) {
         const int sl = base + (oz * BR + oy) * Acc<BR>::kRow + ox;
-        add_fixed32(lo + sl, hi + sl, __float2int_rn(w[0][ox] * wyz), pyz && ok[0][ox]);
+        add_fixed32(lo + sl, hi + sl, __float2int_rn(w[0][ox] * wyz), pyz && ok[0][ox], sink);
       }
     }
 }
@@ -908,7 +908,8 @@ __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, co
 // face r3[d] + 1 gets x_l R_d, at the particle's cell across. lo[d]/hi[d]: field d's words.
 template <int BR>
 __device__ __forceinline__ void deposit_faces(uint32_t *const *lo, uint32_t *const *hi, const int r3[3],
-                                              const float o3[3], const float ru[3], const float *scale) {
+                                              const float o3[3], const float ru[3], const float *scale,
+                                              uint32_t *sink) {
   const bool in0 = (unsigned)r3[0] < (unsigned)BR, in1 = (unsigned)r3[1] < (unsigned)BR,
              in2 = (unsigned)r3[2] < (unsigned)BR;
   const bool acr[3] = {in1 && in2, in0 && in2, in0 && in1};
@@ -918,8 +919,8 @@ __device__ __forceinline__ void deposit_faces(uint32_t *const *lo, uint32_t *con
   for (int d = 0; d < 3; ++d) {
     const float r = ru[d] * scale[1 + d];
     const bool lo_in = (unsigned)r3[d] < (unsigned)BR, hi_in = (unsigned)(r3[d] + 1) < (unsigned)BR;
-    add_fixed32(lo[d] + sl0, hi[d] + sl0, __float2int_rn((1.f - o3[d]) * r), acr[d] && lo_in);
-    add_fixed32(lo[d] + sl0 + step[d], hi[d] + sl0 + step[d], __float2int_rn(o3[d] * r), acr[d] && hi_in);
+    add_fixed32(lo[d] + sl0, hi[d] + sl0, __float2int_rn((1.f - o3[d]) * r), acr[d] && lo_in, sink);
+    add_fixed32(lo[d] + sl0 + step[d], hi[d] + sl0 + step[d], __float2int_rn(o3[d] * r), acr[d] && hi_in, sink);
   }
 }
 
@@ -958,7 +959,7 @@ __device__ __forceinline__ void block_exclusive_scan2(int32_t *a, int n, int32_t
 template <int BR, int NF> struct DepSmem {
   static constexpr int kRanges = Window<BR>::kRanges;
   static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR>::kSlots;
-  static constexpr size_t kBytes = 2 * kAcc + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
+  static constexpr size_t kBytes = 2 * kAcc + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * (40 + 64);
   static_assert(kRanges <= 2 * DepTraits<BR>::kThreads, "ranges exceed the block scan");
 };
 
@@ -985,6 +986,7 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
   int32_t *pre = reinterpret_cast<int32_t *>(acc_hi + NF * SLOTS);  // NR + 1
   int32_t *beg = pre + NR + 1;                                       // NR
   int32_t *misc = beg + NR;                                          // 32 warp sums, item, last
+  uint32_t *sink = reinterpret_cast<uint32_t *>(misc + 40) + (threadIdx.x & 31);  // 2 x 32 words
   uint32_t *lo_f[5], *hi_f[5];
 #pragma unroll
   for (int q = 0; q < 5; ++q) {
@@ -1057,10 +1059,10 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
         // reachable targets: trilinear cells r3 - 1 .. r3 + 1, faces r3 .. r3 + 1 (normal) and r3 (across)
         if (r3[0] >= -1 && r3[0] <= BR && r3[1] >= -1 && r3[1] <= BR && r3[2] >= -1 && r3[2] <= BR) {
           const float o3[3] = {SI.o[0][p], SI.o[1][p], SI.o[2][p]};
-          deposit_trilinear<BR>(lo_f[0], hi_f[0], r3, o3, scale[0]);
+          deposit_trilinear<BR>(lo_f[0], hi_f[0], r3, o3, scale[0], sink);
           if (twc) {
             const float ru[3] = {f.rhs_u[0][p], f.rhs_u[1][p], f.rhs_u[2][p]};
-            deposit_faces<BR>(&lo_f[1], &hi_f[1], r3, o3, ru, scale);
+            deposit_faces<BR>(&lo_f[1], &hi_f[1], r3, o3, ru, scale, sink);
           }
         }
       }
@@ -1072,7 +1074,7 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
         r3[2] = rel_local(ck_(c), b3[2], G.n[2]);
         if (r3[0] >= -1 && r3[0] <= BR && r3[1] >= -1 && r3[1] <= BR && r3[2] >= -1 && r3[2] <= BR) {
           const float o3[3] = {SN.o[0][p], SN.o[1][p], SN.o[2][p]};
-          deposit_trilinear<BR>(lo_f[FE], hi_f[FE], r3, o3, f.rhs_t[p] * scale[4]);
+          deposit_trilinear<BR>(lo_f[FE], hi_f[FE], r3, o3, f.rhs_t[p] * scale[4], sink);
         }
       }
     }
