@@ -98,7 +98,6 @@ struct F32Form {
   float *gas[4];   // ug vg wg at x_int and Tg - t_ref at x_new of the last stage (PSTEP_KEEP_GAS)
   float *drive[4]; // learned correction: the slip (3) and T_new - Tg the last stage's drag and heat transfer used
   uint2 *corr_y;   // learned correction: the network output of the step's stage 0 (bf16 x 4)
-  uint2 *corr_y_tmp;  // its permutation scratch
   float *rhs_u[3];
   float *uf[3], *tf;  // fp32 ghosted copies of the bound fields
   uint32_t *key;      // brick-major cell id of the base position
@@ -1335,14 +1334,8 @@ int sort_step(pstep_ctx *h) {
         put(scr[a], old);
       }
     }
-    if (f.corr_y) {
-      PermBatch<uint2> pb{};
-      pb.src[0] = f.corr_y;
-      pb.dst[0] = f.corr_y_tmp;
-      k_perm_batch<uint2, 1><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n);
-      PSTEP_LAUNCHED(h);
-      uint2 *t = f.corr_y; f.corr_y = f.corr_y_tmp; f.corr_y_tmp = t;
-    }
+    // f.corr_y (the network output) is not carried: stage 0 rewrites it for every
+    // particle before stages 1-3 read it
     PSTEP_CUDA(cudaMemsetAsync(&f.bounds[4], 0, sizeof(uint32_t), h->stream));
     k_max_count<<<1024, kThreads, 0, h->stream>>>(f.cell_start, ncell, &f.bounds[4]);
     PSTEP_LAUNCHED(h);
@@ -1450,7 +1443,7 @@ int f32_destroy(pstep_ctx *h) {
   for (int q = 0; q < 7; ++q) dfree32(f->pp[q]);
   for (int q = 0; q < 4; ++q) dfree32(f->gas[q]);
   for (int q = 0; q < 4; ++q) dfree32(f->drive[q]);
-  dfree32(f->corr_y); dfree32(f->corr_y_tmp);
+  dfree32(f->corr_y);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx);
   dfree32(f->bounds); dfree32(f->se); dfree32(f->slots);
@@ -1678,7 +1671,6 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
     PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
   }
   if (!f.corr_y) TRY32(dalloc32(h, f.corr_y, (size_t)h->cap));
-  if (!f.corr_y_tmp) TRY32(dalloc32(h, f.corr_y_tmp, (size_t)h->cap));
   PSTEP_CUDA(cudaMemsetAsync(f.corr_y, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   h->corr_on = 1;
   return PSTEP_OK;
