@@ -151,6 +151,79 @@ constexpr int kB1 = kB + 1;           // trilinear node region edge [b, b+B]
 constexpr int kB2 = kB + 2;           // face node region edge [b-1, b+B]
 constexpr int kBrickThreads = 256;
 constexpr size_t kBrickSmem = (size_t)kB1 * kB1 * kB1 * (8 + 6) * sizeof(double);
+// A node (or node h-class segment) with more particles than this is summed by a
+// warp: lanes stride its particles in order and a fixed shuffle tree adds the
+// lane sums. The order is fixed by the segment alone, so the result is the same
+// from run to run; one thread walking a blob-centre node (~1000 particles)
+// would hold up its whole brick.
+constexpr int kDenseSeg = 32;
+constexpr int kDenseMax = kB2 * kB2 * kB2;
+
+__device__ __forceinline__ double warp_tree_sum(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;  // lane 0 holds the sum
+}
+
+// The fast deposit sums moments per node instead of the 8 corner weights: with
+// t = (x_l, y_l, z_l) of each particle and value v (1 for the concentration),
+// M[s] = sum v * prod_{d in s} t_d for the 8 subsets s of {x (4), y (2), z (1)}.
+// The corner with (1 - t_d) in the dimensions of bit set o and t_d in the others is
+// sum_{A subset of o} (-1)^|A| M[A | ~o], formed once per node. GB300's FP64 pipe
+// is the bound of this kernel, and per particle this takes 3 + 4 + 8 FP64
+// operations instead of 6 + 3 + 24 (+ 8). x_l = frac + 0.5 - h is formed as
+// frac + (h ? -0.5 : 0.5), the same value (frac - 1 and frac - 0.5 are exact for
+// frac >= 0.5).
+__device__ __forceinline__ void moments_add(double (&m)[8], const DepIn &d, int32_t p, int mode) {
+  const uint32_t key = d.key[p];
+  const double xl = d.frac[0][p] + (((key >> 2) & 1) ? -0.5 : 0.5);
+  const double yl = d.frac[1][p] + (((key >> 1) & 1) ? -0.5 : 0.5);
+  const double zl = d.frac[2][p] + ((key & 1) ? -0.5 : 0.5);
+  const double xy = xl * yl, xz = xl * zl, yz = yl * zl, xyz = xy * zl;
+  if (mode) {
+    const double v = d.val[0][p];
+    m[0] += v;
+    m[4] = fma(xl, v, m[4]);
+    m[2] = fma(yl, v, m[2]);
+    m[1] = fma(zl, v, m[1]);
+    m[6] = fma(xy, v, m[6]);
+    m[5] = fma(xz, v, m[5]);
+    m[3] = fma(yz, v, m[3]);
+    m[7] = fma(xyz, v, m[7]);
+  } else {
+    m[0] += 1.0;
+    m[4] += xl;
+    m[2] += yl;
+    m[1] += zl;
+    m[6] += xy;
+    m[5] += xz;
+    m[3] += yz;
+    m[7] += xyz;
+  }
+}
+
+// corner partial o (bit 2: x takes 1 - x_l, bit 1: y, bit 0: z) from the moments
+__device__ __forceinline__ double corner_of(const double (&m)[8], int o) {
+  const int rest = ~o & 7;
+  double c = 0.0;
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    if ((a & o) != a) continue;  // subsets of o only
+    const double t = m[a | rest];
+    c = (__popc(a) & 1) ? c - t : c + t;
+  }
+  return c;
+}
+
+// face sums of one particle: (sum r, sum t r) per dimension, r = RHS_u component
+__device__ __forceinline__ void face_add(double (&f)[6], const DepIn &d, int32_t p) {
+#pragma unroll
+  for (int D = 0; D < 3; ++D) {
+    const double r = d.val[D][p];
+    f[2 * D] += r;
+    f[2 * D + 1] = fma(d.frac[D][p], r, f[2 * D + 1]);
+  }
+}
 
 __device__ inline int32_t seg_lower_h(const DepIn &d, int32_t a, int32_t b, uint32_t hcls) {
   // first position in [a, b) whose particle has h class >= hcls (segments are sorted by h)
@@ -162,6 +235,13 @@ __device__ inline int32_t seg_lower_h(const DepIn &d, int32_t a, int32_t b, uint
 }
 
 // mode 0: concentration (weights) + face momentum partials at x_int; mode 1: weights * RHS_T
+//
+// A pre-pass tabulates, for every node of the brick's region [b-1, b+B], where its
+// segment starts and where each h class ends inside it (segments are sorted by h):
+// short segments by reading their keys (independent loads), longer ones by binary
+// search, each once per brick rather than once per phase. Nodes whose segment is
+// too long for 16-bit class ends (none at the particle densities of the workloads)
+// fall back to the searches in every phase.
 __global__ void __launch_bounds__(kBrickThreads) k_dep_brick(Geom G, DepIn d, int mode, int twc,
                                                              double *__restrict__ out_tri,
                                                              double *__restrict__ out_x,
@@ -170,77 +250,156 @@ __global__ void __launch_bounds__(kBrickThreads) k_dep_brick(Geom G, DepIn d, in
   extern __shared__ double sm[];
   double *P = sm;                              // [kB1^3][8] trilinear partials of node b + l
   double *F = sm + kB1 * kB1 * kB1 * 8;        // [kB1^3][6] face partials of trunc cell b - 1 + l
+  __shared__ int32_t seg_a[kDenseMax];         // node b - 1 + l: first sorted position
+  __shared__ uint16_t cls_end[kDenseMax][8];   // end of h classes 0..hc, relative to seg_a
+  __shared__ int32_t dense_s[kDenseMax];
+  __shared__ int32_t n_dense;
+  constexpr uint16_t kUntabulated = 0xffffu;
   const int nbx = (G.g[0] + kB - 1) / kB, nby = (G.g[1] + kB - 1) / kB;
   const int bx = (int)(blockIdx.x % nbx) * kB;
   const int by = (int)((blockIdx.x / nbx) % nby) * kB;
   const int bz = (int)(blockIdx.x / ((long long)nbx * nby)) * kB;
+  const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5), nwarps = kBrickThreads / 32;
 
-  // trilinear: per-node partials for nodes [b, b+B]
-  for (int s = threadIdx.x; s < kB1 * kB1 * kB1; s += blockDim.x) {
-    const int lx = s % kB1, ly = (s / kB1) % kB1, lz = s / (kB1 * kB1);
-    const int ni = bx + lx, nj = by + ly, nk = bz + lz;
-    double acc[8];
-#pragma unroll
-    for (int o = 0; o < 8; ++o) acc[o] = 0.0;
+  // pre-pass: segment table of the region's nodes
+  for (int s = threadIdx.x; s < kB2 * kB2 * kB2; s += blockDim.x) {
+    const int lx = s % kB2, ly = (s / kB2) % kB2, lz = s / (kB2 * kB2);
+    const int ni = bx - 1 + lx, nj = by - 1 + ly, nk = bz - 1 + lz;
+    int32_t a0 = 0, cnt = 0;
     if (node_ok(G, ni, nj, nk)) {
       const long long n = glin(G, ni, nj, nk);
-      const int32_t a = d.cell_start[n], e = d.cell_start[n + 1];
-      for (int32_t q = a; q < e; ++q) {
-        const int32_t p = pidx(d, q);
-        const uint32_t key = d.key[p];
-        const double xl = xl_round(d.frac[0][p], (key >> 2) & 1);
-        const double yl = xl_round(d.frac[1][p], (key >> 1) & 1);
-        const double zl = xl_round(d.frac[2][p], key & 1);
-        const double v = mode ? d.val[0][p] : 1.0;
-#pragma unroll
-        for (int o = 0; o < 8; ++o) {
-          const double fx = (o & 4) ? (1 - xl) : xl;
-          const double fy = (o & 2) ? (1 - yl) : yl;
-          const double fz = (o & 1) ? (1 - zl) : zl;
-          double w = fx * fy * fz;
-          if (mode) w = w * v;
-          acc[o] += w;
-        }
-      }
+      a0 = d.cell_start[n];
+      cnt = d.cell_start[n + 1] - a0;
     }
+    seg_a[s] = a0;
+    if (cnt <= 16) {
+      uint64_t c = 0;  // 8 one-byte class counts (at most 16 each)
+      for (int32_t q = 0; q < cnt; ++q) c += 1ull << (8u * (d.key[pidx(d, a0 + q)] & 7u));
+      int run = 0;
 #pragma unroll
-    for (int o = 0; o < 8; ++o) P[s * 8 + o] = acc[o];
+      for (int hc = 0; hc < 8; ++hc) {
+        run += (int)((c >> (8 * hc)) & 0xffu);
+        cls_end[s][hc] = (uint16_t)run;
+      }
+    } else if (cnt < (int32_t)kUntabulated) {
+#pragma unroll 1
+      for (int hc = 0; hc < 7; ++hc) cls_end[s][hc] = (uint16_t)(seg_lower_h(d, a0, a0 + cnt, hc + 1) - a0);
+      cls_end[s][7] = (uint16_t)cnt;
+    } else {
+      cls_end[s][7] = kUntabulated;
+    }
+  }
+  if (threadIdx.x == 0) n_dense = 0;
+  __syncthreads();
+  // [a, e) of node slot s (region index) and h class hc
+  auto seg = [&](int s, int hc, int32_t &a, int32_t &e) {
+    const int32_t a0 = seg_a[s];
+    if (cls_end[s][7] != kUntabulated) {
+      a = a0 + (hc ? cls_end[s][hc - 1] : 0);
+      e = a0 + cls_end[s][hc];
+    } else {  // a segment longer than the table holds
+      const int lx = s % kB2, ly = (s / kB2) % kB2, lz = s / (kB2 * kB2);
+      const long long n = glin(G, bx - 1 + lx, by - 1 + ly, bz - 1 + lz);
+      const int32_t e0 = d.cell_start[n + 1];
+      a = hc ? seg_lower_h(d, a0, e0, hc) : a0;
+      e = hc < 7 ? seg_lower_h(d, a, e0, hc + 1) : e0;
+    }
+  };
+  // whole segment of node slot s
+  auto whole = [&](int s, int32_t &a, int32_t &e) {
+    int32_t a1, e1;
+    seg(s, 0, a, e1);
+    seg(s, 7, a1, e);
+  };
+
+  // trilinear: per-node partials for nodes [b, b+B] (region slot = l + 1); dense nodes listed for the warps
+  for (int s = threadIdx.x; s < kB1 * kB1 * kB1; s += blockDim.x) {
+    const int lx = s % kB1, ly = (s / kB1) % kB1, lz = s / (kB1 * kB1);
+    const int rs = ((lz + 1) * kB2 + (ly + 1)) * kB2 + (lx + 1);
+    double m[8];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) m[o] = 0.0;
+    int32_t a, e;
+    whole(rs, a, e);
+    if (e - a > kDenseSeg) {
+      dense_s[atomicAdd(&n_dense, 1)] = s;
+      continue;
+    }
+    // one path for every node (empty ones included): the FP64 pipe is charged per warp
+    // instruction, so lanes on different paths would cost the warp both
+    for (int32_t q = a; q < e; ++q) moments_add(m, d, pidx(d, q), mode);
+#pragma unroll
+    for (int o = 0; o < 8; ++o) P[s * 8 + o] = corner_of(m, o);
+  }
+  __syncthreads();
+  for (int k = warp; k < n_dense; k += nwarps) {
+    const int s = dense_s[k];
+    const int lx = s % kB1, ly = (s / kB1) % kB1, lz = s / (kB1 * kB1);
+    int32_t a, e;
+    whole(((lz + 1) * kB2 + (ly + 1)) * kB2 + (lx + 1), a, e);
+    double m[8];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) m[o] = 0.0;
+    for (int32_t q = a + lane; q < e; q += 32) moments_add(m, d, pidx(d, q), mode);
+#pragma unroll
+    for (int o = 0; o < 8; ++o) m[o] = warp_tree_sum(m[o]);
+    if (lane == 0) {
+#pragma unroll
+      for (int o = 0; o < 8; ++o) P[s * 8 + o] = corner_of(m, o);
+    }
   }
   const bool faces = (mode == 0) && twc;
   if (faces) {
     for (int s = threadIdx.x; s < kB1 * kB1 * kB1 * 6; s += blockDim.x) F[s] = 0.0;
   }
   __syncthreads();
-  // face partials: trunc cell c = node - h, one h class per phase (distinct nodes -> distinct cells)
+  // face partials: trunc cell c = node - h, one h class per phase (distinct nodes -> distinct cells);
+  // dense segments listed for the warps as above
   if (faces) {
-    for (uint32_t hc = 0; hc < 8; ++hc) {
+    for (int hc = 0; hc < 8; ++hc) {
       const int hx = (hc >> 2) & 1, hy = (hc >> 1) & 1, hz = hc & 1;
+      if (threadIdx.x == 0) n_dense = 0;
+      __syncthreads();
       for (int s = threadIdx.x; s < kB2 * kB2 * kB2; s += blockDim.x) {
         const int lx = s % kB2, ly = (s / kB2) % kB2, lz = s / (kB2 * kB2);
         const int cx = lx - hx, cy = ly - hy, cz = lz - hz;  // cell slot: cell = b - 1 + c
         if (cx < 0 || cy < 0 || cz < 0 || cx >= kB1 || cy >= kB1 || cz >= kB1) continue;
-        const int ni = bx - 1 + lx, nj = by - 1 + ly, nk = bz - 1 + lz;
-        if (!node_ok(G, ni, nj, nk)) continue;
-        const long long n = glin(G, ni, nj, nk);
-        const int32_t a0 = d.cell_start[n], e0 = d.cell_start[n + 1];
-        if (a0 == e0) continue;
-        const int32_t a = seg_lower_h(d, a0, e0, hc);
-        const int32_t e = seg_lower_h(d, a, e0, hc + 1);
+        int32_t a, e;
+        seg(s, hc, a, e);
         if (a == e) continue;
-        double s0x = 0, s1x = 0, s0y = 0, s1y = 0, s0z = 0, s1z = 0;
-        for (int32_t q = a; q < e; ++q) {
-          const int32_t p = pidx(d, q);
-          const double xl = d.frac[0][p], yl = d.frac[1][p], zl = d.frac[2][p];
-          const double ru = d.val[0][p], rv = d.val[1][p], rw = d.val[2][p];
-          s1x += xl * ru;
-          s0x += (1 - xl) * ru;
-          s1y += yl * rv;
-          s0y += (1 - yl) * rv;
-          s1z += zl * rw;
-          s0z += (1 - zl) * rw;
+        if (e - a > kDenseSeg) {
+          dense_s[atomicAdd(&n_dense, 1)] = s;
+          continue;
         }
+        double fs[6] = {0, 0, 0, 0, 0, 0};
+        for (int32_t q = a; q < e; ++q) face_add(fs, d, pidx(d, q));
+        // (1 - x_l) r summed as sum r - sum x_l r; x_l r as is
         double *f = F + ((cz * kB1 + cy) * kB1 + cx) * 6;
-        f[0] += s0x; f[1] += s1x; f[2] += s0y; f[3] += s1y; f[4] += s0z; f[5] += s1z;
+#pragma unroll
+        for (int D = 0; D < 3; ++D) {
+          f[2 * D] += fs[2 * D] - fs[2 * D + 1];
+          f[2 * D + 1] += fs[2 * D + 1];
+        }
+      }
+      __syncthreads();
+      for (int k = warp; k < n_dense; k += nwarps) {
+        const int s = dense_s[k];
+        const int lx = s % kB2, ly = (s / kB2) % kB2, lz = s / (kB2 * kB2);
+        const int cx = lx - hx, cy = ly - hy, cz = lz - hz;
+        int32_t a, e;
+        seg(s, hc, a, e);
+        double fs[6] = {0, 0, 0, 0, 0, 0};
+        for (int32_t q = a + lane; q < e; q += 32) face_add(fs, d, pidx(d, q));
+#pragma unroll
+        for (int j = 0; j < 6; ++j) fs[j] = warp_tree_sum(fs[j]);
+        if (lane == 0) {
+          double *f = F + ((cz * kB1 + cy) * kB1 + cx) * 6;
+#pragma unroll
+          for (int D = 0; D < 3; ++D) {
+            f[2 * D] += fs[2 * D] - fs[2 * D + 1];
+            f[2 * D + 1] += fs[2 * D + 1];
+          }
+        }
       }
       __syncthreads();
     }
