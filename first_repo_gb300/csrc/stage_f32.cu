@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
 // stages 1-3 with the correction: the network output of the step's stage 0, applied with
 // this stage's drive slip and prior
 template <int K>
-__global__ void __launch_bounds__(256) k_advance32_corr(Geom G, F32Form f, C32 c, int twc, int64_t n,
+__global__ void __launch_bounds__(256, 5) k_advance32_corr(Geom G, F32Form f, C32 c, int twc, int64_t n,
                                                         int32_t *__restrict__ err, CorrDev cd) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
