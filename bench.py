@@ -87,6 +87,21 @@ def rank_info():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The largest value over the ranks (the timed region's time is the slowest rank's)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, n_per_rank: int, ms_per_step: float) -> float:
+    """Whole-job particle-steps/s: every rank steps its own replica of n particles."""
+    return world * n_per_rank / (ms_per_step / 1e3)
+
+
 class Clocks:
     """nvidia-smi sampled every 200 ms while the timed region runs."""
 
@@ -305,13 +320,9 @@ def main():
     launches = g.launches() - l0
     prof = g.profile_read()
     g.profile(False)
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, "cuda")
     ms_per_step = ms / args.steps
-    value = world * n / (ms_per_step / 1e3)
+    value = job_rate(world, n, ms_per_step)
 
     # roofline of the dominant phase (live CUDA-event time of its launches in the timed region)
     peak, peak_kind = peaks()
@@ -370,10 +381,10 @@ def main():
         for _ in range(ke):
             one_step()
         barrier()
-        e2e_s = (time.perf_counter() - t0) / ke
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, dist, "cuda")
         h2d = sum(a.nbytes for a in hin) + sum(f.nbytes for f in hf)
         d2h = sum(a.nbytes for a in hout) + sum(f.nbytes for f in out_f)
-        e2e = {"value": world * n / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+        e2e = {"value": job_rate(world, n, e2e_s * 1e3), "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                "loop": "host time-stepping: each step's particles read back are the next step's inputs"}
         del C
