@@ -80,6 +80,16 @@ def test_null_handle_is_an_error(built_cuda):
     assert L.pstep_prime(None) == 1
     assert L.pstep_end_step(None) == 1
     assert L.pstep_num_particles(None) == -1
+    # statistics and snapshot files (no device is touched for these argument checks)
+    v64, d = ctypes.c_int64(), ctypes.c_double()
+    assert L.pstep_np_tot(None, ctypes.byref(v64)) == 1
+    assert L.pstep_max(None, 0, ctypes.byref(d)) == 1
+    assert L.pstep_balance_index(None, ctypes.byref(d)) == 1
+    assert L.pstep_field_stats(None, 0, None, None, None) == 1
+    assert L.pstep_find_tags(None, None, 0, None, None) == 1
+    assert L.pstep_store_all(None, b"./", 0) == 1
+    assert L.pstep_load_all(None, b"./", 1, 1) == 1
+    assert L.pstep_status_string(11) == b"snapshot file error"
 
 
 REFDIR = "/root/reference"
