@@ -1511,7 +1511,9 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
   for (int64_t c = 0, p0 = 0; p0 < n; ++c, p0 += kStageChunk) {
     const int sl = (int)(c & 1);
     const int64_t len = n - p0 < kStageChunk ? n - p0 : kStageChunk;
-    if (c >= 2) PSTEP_CUDA(cudaStreamWaitEvent(f.copy_stream, f.ev_used[sl], 0));  // slot's last conversion done
+    // the slot's last conversion (of this upload, or of an earlier upload or read-back
+    // still running on the handle's stream) is done; an event never recorded is complete
+    PSTEP_CUDA(cudaStreamWaitEvent(f.copy_stream, f.ev_used[sl], 0));
     double *b = f.stage[sl];
     for (int q = 0; q < 7; ++q)
       PSTEP_CUDA(cudaMemcpyAsync(b + q * kStageChunk, src[q] + p0, sizeof(double) * len, cudaMemcpyHostToDevice,
@@ -1881,7 +1883,7 @@ int f32_get_array(pstep_ctx *h, int id, void *dst, int on_device) {
   for (int64_t c = 0, p0 = 0; p0 < n; ++c, p0 += kStageChunk) {
     const int sl = (int)(c & 1);
     const int64_t len = n - p0 < kStageChunk ? n - p0 : kStageChunk;
-    if (c >= 2) PSTEP_CUDA(cudaStreamWaitEvent(h->stream, f.ev_copied[sl], 0));  // slot's last copy done
+    PSTEP_CUDA(cudaStreamWaitEvent(h->stream, f.ev_copied[sl], 0));  // the slot's last copy (any call) is done
     convert(p0, len, f.stage[sl]);
     PSTEP_LAUNCHED(h);
     PSTEP_CUDA(cudaEventRecord(f.ev_used[sl], h->stream));

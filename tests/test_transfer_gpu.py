@@ -40,3 +40,29 @@ def test_fp32_host_round_trip_over_several_chunks(built_cuda):
         d = (got - a + L / 2) % L - L / 2
         assert np.max(np.abs(d)) <= dx * 2.0 ** -23, name
     g.close()
+
+
+def test_fp32_back_to_back_host_uploads(built_cuda):
+    """Two uploads in a row (the second's copies must wait for the first's conversions
+    still running on the handle's stream), then a read-back: the second population."""
+    n, count = 64, STAGE_CHUNK + 77
+    bp = helpers.make_bp(n, count)
+    L = bp.l
+    rng = np.random.default_rng(11)
+    pops = []
+    for _ in range(2):
+        x, y, z = (rng.uniform(0.0, L, count) for _ in range(3))
+        u, v, w = (rng.normal(0.0, 1.0, count) for _ in range(3))
+        t = rng.uniform(0.5, 2.0, count)
+        flag = rng.permutation(count).astype(np.int32)
+        pops.append((x, y, z, u, v, w, t, flag))
+    g = pstep.ParticleStep(bp.step_config(), count, pstep.FP32, 0)
+    for pop in pops:
+        g.load(*pop)
+    x, y, z, u, v, w, t, flag = pops[1]
+    assert np.array_equal(g.array("flag"), flag)
+    assert np.array_equal(g.array("u"), u.astype(np.float32).astype(np.float64))
+    dx = L / n
+    d = (g.array("x") - x + L / 2) % L - L / 2
+    assert np.max(np.abs(d)) <= dx * 2.0 ** -23
+    g.close()
