@@ -242,6 +242,9 @@ int pstep_find_tags(pstep_handle h, const int32_t *tags, int32_t n, double *xyz,
   if (!rc) {
     for (auto &v : idx)
       if (v == INT32_MAX) v = -1;
+    // an id asked for more than once: only its first sorted copy was searched for
+    for (int32_t q = 1; q < n; ++q)
+      if (sorted[(size_t)q] == sorted[(size_t)q - 1]) idx[(size_t)q] = idx[(size_t)q - 1];
     cudaError_t e = cudaMemcpyAsync(d_idx, idx.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) rc = fail_io(h, PSTEP_ERR_CUDA, std::string("find_tags: ") + cudaGetErrorString(e));
   }

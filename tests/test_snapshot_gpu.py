@@ -98,11 +98,13 @@ def test_fp32_snapshot_round_trip_and_statistics(built_cuda, tmp_path):
     for k in KEYS:
         assert g.max(k) == pyoracle.array_max(got[k]), k
     _check_field_stats(g)
-    xyz, found = g.find_tags([0, 11, COUNT - 1, -5])
+    tags = [0, 11, COUNT - 1, -5, 11]  # an absent id and a repeated one
+    xyz, found = g.find_tags(tags)
     where = {int(f): i for i, f in enumerate(got["flag"])}
-    assert list(found) == [True, True, True, False]
-    for i, t in enumerate([0, 11, COUNT - 1]):
-        assert [xyz[i, dd] for dd in range(3)] == [got[k][where[t]] for k in ("x", "y", "z")]
+    assert list(found) == [True, True, True, False, True]
+    for i, t in enumerate(tags):
+        if found[i]:
+            assert [xyz[i, dd] for dd in range(3)] == [got[k][where[t]] for k in ("x", "y", "z")]
     bp = helpers.make_bp(N, COUNT)
     g2 = pstep.ParticleStep(bp.step_config(), COUNT, pstep.FP32, 0)
     g2.load_all(d, COUNT)
