@@ -95,7 +95,8 @@ def test_port_matches_reference_binary(built, n, count, steps, clustered, seed):
 
 def test_known_answer_uniform_temperature(built):
     """Uniform gas T and zero gas velocity: T_p follows RK4 of dT/dt = (Tg - T)/tau_T + Q
-    and u_p of du/dt = -u/tau_p (known answers from the mathematics)."""
+    and u_p of du/dt = -u/tau_p; the deposits conserve particle count, momentum and
+    energy (known answers from the mathematics)."""
     n, count = 8, 64
     bp = helpers.make_bp(n, count)
     cfg = bp.step_config()
@@ -129,3 +130,9 @@ def test_known_answer_uniform_temperature(built):
     assert abs(c.sum() - count) < 1e-10
     e = o.fields["E"][1:-1, 1:-1, 1:-1]
     assert abs(e.sum() - o.array("RHS_T").sum()) < 1e-12 * max(1.0, abs(e).sum())
+    # deposited momentum sums to the sum of RHS_u per component (the face weights of a
+    # particle add to one: x_l + (1 - x_l), particle.cpp:498-524)
+    for comp, key in (("Ax", "RHS_u"), ("Ay", "RHS_v"), ("Az", "RHS_w")):
+        a, r = o.fields[comp][1:-1, 1:-1, 1:-1], o.array(key)
+        assert abs(a.sum() - r.sum()) < 1e-12 * max(1.0, np.abs(r).sum()), comp
+    assert np.abs(o.array("RHS_u")).sum() > 0
