@@ -281,9 +281,8 @@ def run_ref_snapshot(bp, case: dict, nsteps: int, workdir: str, store_ts: int = 
     """Run the harness with Store_All (store_ts >= 0), statistics and trajectory
     (np_track > 0, statistics on) and/or Load_All (load: Restart_Part_*.bin in workdir).
     Returns the records, the STATS line and the trajectory rows (time, then x y z per id)."""
-    if not os.path.exists(REF_BIN):
-        if build_ref() is None:
-            raise RuntimeError("reference sources are not available here")
+    if build_ref() is None:  # incremental: rebuilds only when the harness or its sources changed
+        raise RuntimeError("reference sources are not available here")
     pfile, ifile = write_case(workdir, bp, case)
     if np_track:
         lines = open(pfile).read().split("\n")
@@ -309,9 +308,8 @@ def run_ref_snapshot(bp, case: dict, nsteps: int, workdir: str, store_ts: int = 
 
 def run_ref(bp, case: dict, nsteps: int, dump_all: bool = True, timing: bool = False, workdir: str | None = None):
     """Run the reference's own particle step (oracle/_ref/ref_harness) on a case."""
-    if not os.path.exists(REF_BIN):
-        if build_ref() is None:
-            raise RuntimeError("reference sources are not available here")
+    if build_ref() is None:  # incremental: rebuilds only when the harness or its sources changed
+        raise RuntimeError("reference sources are not available here")
     own = workdir is None
     d = workdir or tempfile.mkdtemp(prefix="pstep_ref_")
     pfile, ifile = write_case(d, bp, case)
