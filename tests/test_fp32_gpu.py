@@ -160,3 +160,26 @@ def test_fp32_dense_blob_split_bricks(built_cuda, n, count, br):
         g.close()
     for a, b in zip(*outs):
         assert helpers.bits_equal(a, b)
+
+
+def test_fp32_empty_population(built_cuda):
+    """No particles: the step runs, every deposited field is zero, the arrays are empty."""
+    n = 16
+    bp = helpers.make_bp(n, 100)
+    ux, uy, uz = gen.velocity(n, 41)
+    tf = gen.temperature(n, 42)
+    fields = [gen.ghost(a) for a in (ux, uy, uz, tf)]
+    g = pstep.ParticleStep(bp.step_config(), 16, pstep.FP32, 0)
+    empty = np.zeros(0)
+    g.load(empty, empty, empty, empty, empty, empty, empty, np.zeros(0, dtype=np.int32))
+    g.bind_velocity(*fields[:3])
+    g.bind_temperature(fields[3])
+    g.prime()
+    g.run(2)
+    rc, flags = g.check()
+    assert rc == 0, flags
+    for f in FIELDS:
+        assert not np.any(g.field(helpers.FIELD_MAP[f])), f
+    assert g.array("x").size == 0 and g.array("flag").size == 0
+    assert g.np_tot() == 0 and g.max("u") == -1e9
+    g.close()
