@@ -618,11 +618,9 @@ bool reference_sums(const pstep_ctx *h) {
 
 int brick_launch(pstep_ctx *h, const DepIn &d, int mode, double *tri, double *ox, double *oy, double *oz) {
   const Geom &G = h->geom;
-  static bool attr = false;
-  if (!attr) {
-    PSTEP_CUDA(cudaFuncSetAttribute(k_dep_brick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBrickSmem));
-    attr = true;
-  }
+  // the opt-in applies to the current device, which is the one this launch uses;
+  // setting it at every launch keeps it right for handles on several devices
+  PSTEP_CUDA(cudaFuncSetAttribute(k_dep_brick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBrickSmem));
   const long long nb = (long long)((G.g[0] + kB - 1) / kB) * ((G.g[1] + kB - 1) / kB) * ((G.g[2] + kB - 1) / kB);
   k_dep_brick<<<(unsigned)nb, kBrickThreads, kBrickSmem, h->stream>>>(G, d, mode, h->cfg.twc, tri, ox, oy, oz);
   PSTEP_LAUNCHED(h);

@@ -21,7 +21,9 @@ static __device__ __align__(256) double g_row_sums[kNoallocMaxRows];
 
 double *g_row_addr[kMaxDevices] = {nullptr};
 std::mutex g_row_mutex;
-char g_noalloc_err[256] = "";
+// one message buffer per calling thread, so that two threads failing at once
+// each read their own message
+thread_local char g_noalloc_err[256] = "";
 
 // one warp per row: fixed-order sum of the row's interior cells
 __global__ void k_row_sums(const double *__restrict__ f, int nx, int ny, int nz, double *__restrict__ rows) {
@@ -76,11 +78,26 @@ extern "C" int pstep_field_mean_noalloc(const double *field, int32_t nx, int32_t
     snprintf(g_noalloc_err, sizeof g_noalloc_err, "no usable current CUDA device");
     return PSTEP_ERR_CUDA;
   }
+  cudaStream_t s = (cudaStream_t)stream;
   double *rows = nullptr;
   {
     // set-up, once per device, with that device current: the device address of the scratch array
     std::lock_guard<std::mutex> lock(g_row_mutex);
     if (!g_row_addr[dev]) {
+      // the look-up is not a stream operation and may end a capture in progress: refuse
+      // cleanly instead, the caller makes one call on this device before capturing
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        snprintf(g_noalloc_err, sizeof g_noalloc_err, "cudaStreamIsCapturing failed");
+        return PSTEP_ERR_CUDA;
+      }
+      if (cs != cudaStreamCaptureStatusNone) {
+        snprintf(g_noalloc_err, sizeof g_noalloc_err,
+                 "first call on device %d made while its stream is being captured: make one call before capture",
+                 dev);
+        return PSTEP_ERR_STATE;
+      }
       cudaError_t e = cudaGetSymbolAddress((void **)&g_row_addr[dev], g_row_sums);
       if (e != cudaSuccess) {
         g_row_addr[dev] = nullptr;
@@ -91,7 +108,6 @@ extern "C" int pstep_field_mean_noalloc(const double *field, int32_t nx, int32_t
     }
     rows = g_row_addr[dev];
   }
-  cudaStream_t s = (cudaStream_t)stream;
   const int threads = 256;
   const int64_t blocks = (nrows * 32 + threads - 1) / threads;
   k_row_sums<<<(unsigned)blocks, threads, 0, s>>>(field, nx, ny, nz, rows);

@@ -1662,12 +1662,6 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
   cd.dp_per_itth = (cfg.nu > 0 && cfg.k > 0) ? (float)(1.0 / (cfg.nu * kPi * cfg.k)) : 0.f;
   cd.dp = (float)cfg.dp;
   cd.idx = (float)G.idx[0];
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_advance32_mlp<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc);
-    PSTEP_CUDA(cudaGetLastError());
-    attr = true;
-  }
   for (int q = 0; q < 4; ++q) {
     if (!f.drive[q]) TRY32(dalloc32(h, f.drive[q], (size_t)h->cap));
     PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
@@ -1721,6 +1715,9 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
       // the network: persistent CTAs of two warpgroups, 3 per SM, tiles of 128 particles
       const int64_t pairs = (n + 2 * corr::kRows - 1) / (2 * corr::kRows);
       const unsigned grid = (unsigned)(pairs < 3 * (int64_t)h->num_sms ? pairs : 3 * (int64_t)h->num_sms);
+      // the shared-memory opt-in belongs to the current (launch) device: set it per launch
+      PSTEP_CUDA(cudaFuncSetAttribute(k_advance32_mlp<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)corr::kAlloc));
       k_advance32_mlp<0><<<grid, corr::kThreads, corr::kAlloc, h->stream>>>(h->geom, f, c, h->cfg.twc, n,
                                                                             h->err_word, cd);
     } else if (k == 1) {

@@ -235,9 +235,10 @@ int pstep_get_particle_array(pstep_handle h, int array_id, void *dst, int on_dev
  * scratch is a fixed device array of 2^20 row sums (8 MiB, held by every GPU that
  * loads the library until the process exits): ny*nz above 2^20 returns
  * PSTEP_ERR_CAPACITY. The first call on a device looks up that array's address
- * (make it before any stream capture). Every call writes all the scratch it reads,
+ * (make it before any stream capture: a first call on a capturing stream returns
+ * PSTEP_ERR_STATE and launches nothing). Every call writes all the scratch it reads,
  * so nothing needs clearing, but all calls share the array: calls that overlap on
- * the GPU race. Messages: pstep_noalloc_last_error(). */
+ * the GPU race. Messages: pstep_noalloc_last_error(), per calling thread. */
 int pstep_field_mean_noalloc(const double *field, int32_t nx, int32_t ny, int32_t nz, double *out, void *stream);
 const char *pstep_noalloc_last_error(void);
 

@@ -20,7 +20,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libpstep_oracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
-REFDIR = "/root/reference"
+# where the reference's sources lie: PSTEP_REFERENCE_DIR, else this build container's
+# mount point; everything that needs them is skipped where the directory is absent
+REFDIR = os.environ.get("PSTEP_REFERENCE_DIR", "/root/reference")
 
 ARRAYS = ["x", "y", "z", "x_int", "y_int", "z_int", "x_new", "y_new", "z_new", "x_np1", "y_np1", "z_np1",
           "u", "v", "w", "u_int", "v_int", "w_int", "u_new", "v_new", "w_new", "u_np1", "v_np1", "w_np1",

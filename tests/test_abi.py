@@ -8,6 +8,7 @@ import subprocess
 import pytest
 
 import helpers  # noqa: F401  (sets sys.path)
+import pyoracle
 from first_repo_gb300 import _lib, gas, mlp, pstep
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -92,7 +93,7 @@ def test_null_handle_is_an_error(built_cuda):
     assert L.pstep_status_string(11) == b"snapshot file error"
 
 
-REFDIR = "/root/reference"
+REFDIR = pyoracle.REFDIR  # PSTEP_REFERENCE_DIR, skipped where absent
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(REFDIR, "particle.h")), reason="reference headers not present")

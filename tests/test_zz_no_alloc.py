@@ -47,6 +47,18 @@ def test_field_mean_noalloc_matches_energy_mean(built_cuda):
         assert abs(got - want) <= MEAN_RTOL * abs(want), (got, want)
         means.append(got)
     assert means[0] != means[1]
+    # a non-cubic field with non-zero ghost layers: the interior of a (nz+2, ny+2, nx+2)
+    # array, axes in the reference's layout (i fastest), against numpy
+    nx, ny, nz = 5, 7, 3
+    rng = np.random.default_rng(5)
+    host = rng.standard_normal((nz + 2, ny + 2, nx + 2)) + 10.0 * np.arange(nz + 2)[:, None, None]
+    host[1:-1, 1:-1, 1:-1] += np.arange(nx)[None, None, :] * 0.25 + np.arange(ny)[None, :, None] * 0.5
+    small = torch.from_numpy(host.ravel().copy()).to("cuda")
+    rc = L.pstep_field_mean_noalloc(C.c_void_p(small.data_ptr()), nx, ny, nz, C.c_void_p(out.data_ptr()), None)
+    assert rc == 0, L.pstep_noalloc_last_error()
+    torch.cuda.synchronize()
+    want = host[1:-1, 1:-1, 1:-1].mean()
+    assert abs(float(out.item()) - want) <= MEAN_RTOL * abs(want), (float(out.item()), want)
     # beyond the fixed scratch: a clear error, nothing launched
     rc = L.pstep_field_mean_noalloc(C.c_void_p(field.data_ptr()), 4, 2048, 1024, C.c_void_p(out.data_ptr()), None)
     assert rc == 3 and b"exceeds" in L.pstep_noalloc_last_error()
