@@ -183,6 +183,125 @@ def pinned_like(a: np.ndarray) -> np.ndarray:
     return out
 
 
+def fp32_error_report(g32, g64, L: float, n_cells: int) -> dict:
+    """The FP32 form's error against the FP64 step run on the same inputs for the same
+    number of steps, matched by particle id and computed on the device:
+      position_cells_max       max over particles of |x32 - x64| (periodic) in cell units
+      velocity_rel_max / _p999 per particle |u32 - u64| / |u64| (velocity vectors)
+      temperature_rel_max      per particle |T32 - T64| / |T64|
+      rhs_t_rel_to_max         max |RHS_T32 - RHS_T64| / max |RHS_T64|
+      fields                   per deposited field max |f32 - f64| / max |f64| (C: interior)
+      energy_mean_rel          |mean32 - mean64| / |mean64|
+      momentum_rel_to_abs      per component |sum32 - sum64| / sum |RHS_RU64| over the interior
+    """
+    import torch
+    dev = "cuda"
+    n = g32.np
+    if g64.np != n:
+        raise ValueError("populations differ in size")
+
+    def arr(g, name, dtype=torch.float64):
+        t = torch.empty(n, dtype=dtype, device=dev)
+        g.array(name, out=t)
+        return t
+
+    i32 = torch.argsort(arr(g32, "flag", torch.int32))
+    i64 = torch.argsort(arr(g64, "flag", torch.int32))
+    if not torch.equal(arr(g32, "flag", torch.int32)[i32], arr(g64, "flag", torch.int32)[i64]):
+        raise ValueError("particle ids differ")
+    rep = {}
+    dx = L / n_cells
+    pos = 0.0
+    for k in ("x", "y", "z"):
+        d = arr(g32, k)[i32] - arr(g64, k)[i64]
+        d = torch.remainder(d + L / 2, L) - L / 2
+        pos = max(pos, float(d.abs().max()) / dx)
+    rep["position_cells_max"] = pos
+    du = torch.zeros(n, dtype=torch.float64, device=dev)
+    sp = torch.zeros(n, dtype=torch.float64, device=dev)
+    for k in ("u", "v", "w"):
+        a, b = arr(g32, k)[i32], arr(g64, k)[i64]
+        du += (a - b) ** 2
+        sp += b ** 2
+        del a, b
+    rel = torch.sqrt(du) / torch.sqrt(sp).clamp_min(1e-300)
+    rep["velocity_rel_max"] = float(rel.max())
+    rep["velocity_rel_p999"] = float(torch.quantile(rel[torch.randperm(n, device=dev)[: 1 << 22]], 0.999))
+    del du, sp, rel
+    a, b = arr(g32, "T")[i32], arr(g64, "T")[i64]
+    rep["temperature_rel_max"] = float(((a - b).abs() / b.abs().clamp_min(1e-300)).max())
+    a, b = arr(g32, "RHS_T")[i32], arr(g64, "RHS_T")[i64]
+    rep["rhs_t_rel_to_max"] = float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+    del a, b
+    g = n_cells + 2
+    fields = {}
+    mom = {}
+    s32, s64 = g32.momentum_sums(), g64.momentum_sums()
+    for i, name in enumerate(("C", "RHS_RU_x", "RHS_RU_y", "RHS_RU_z", "RHS_Part_Temp")):
+        a = torch.empty(g ** 3, dtype=torch.float64, device=dev)
+        b = torch.empty(g ** 3, dtype=torch.float64, device=dev)
+        g32.field(name, out=a)
+        g64.field(name, out=b)
+        a = a.view(g, g, g)[1:-1, 1:-1, 1:-1]
+        b = b.view(g, g, g)[1:-1, 1:-1, 1:-1]
+        fields[name] = float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+        if 1 <= i <= 3:
+            mom[name] = abs(s32[i - 1] - s64[i - 1]) / max(float(b.abs().sum()), 1e-300)
+        del a, b
+    rep["fields"] = fields
+    rep["momentum_rel_to_abs"] = mom
+    e32, e64 = g32.energy_mean(), g64.energy_mean()
+    rep["energy_mean_rel"] = abs(e32 - e64) / max(abs(e64), 1e-300)
+    torch.cuda.empty_cache()
+    return rep
+
+
+def particle_stats(g, u_fields_dev, L: float, n_cells: int) -> dict:
+    """Slip-velocity and particle-temperature statistics of a population, on the device:
+    the slip is u_p - U(x_p) with U the bound gas velocity interpolated at the particle's
+    position as gas2part_velocity does (particle.cpp:340-360: face-normal linear, ghosted
+    index (int)(x/dx) + 1). u_fields_dev: the three ghosted velocity fields as flat fp64
+    device tensors."""
+    import torch
+    dev = "cuda"
+    n = g.np
+    gs = n_cells + 2
+    idx = n_cells / L
+
+    def arr(name):
+        t = torch.empty(n, dtype=torch.float64, device=dev)
+        g.array(name, out=t)
+        return t
+
+    pos = [arr(k) for k in ("x", "y", "z")]
+    # clamped into the ghosted range so that no index can leave the arrays (a position at
+    # x = L, which the FP64 form flags as out of range, reads the last interior face pair)
+    cell = [torch.floor(p * idx).clamp(0, n_cells - 1) for p in pos]
+    frac = [(p * idx - c).clamp(0.0, 1.0) for p, c in zip(pos, cell)]
+    ci = [c.to(torch.int64) + 1 for c in cell]
+    del pos, cell
+    slip2 = torch.zeros(n, dtype=torch.float64, device=dev)
+    for d, name in enumerate(("u", "v", "w")):
+        lo = (ci[2] * gs + ci[1]) * gs + ci[0]
+        step = (1, gs, gs * gs)[d]
+        f = u_fields_dev[d]
+        ug = frac[d] * f[lo + step] + (1 - frac[d]) * f[lo]
+        slip2 += (arr(name) - ug) ** 2
+        del lo, ug
+    t = arr("T")
+    out = {"slip_rms": float(torch.sqrt(slip2.mean())), "slip_mean": float(torch.sqrt(slip2).mean()),
+           "T_mean": float(t.mean()), "T_rms": float(torch.sqrt(((t - t.mean()) ** 2).mean())),
+           "T_max": float(t.max())}
+    del slip2, t, frac, ci
+    torch.cuda.empty_cache()
+    return out
+
+
+def stats_difference(a: dict, b: dict) -> dict:
+    """a - b and (a - b) / |b| for each statistic"""
+    return {k: {"diff": a[k] - b[k], "rel": (a[k] - b[k]) / abs(b[k]) if b[k] else None} for k in a}
+
+
 def cpu_sample_rate(n_cells=160, count=1 << 22, steps=2, seed=77, clustered=True):
     """Oracle (single thread) on a bounded sample with the workload's density and construction."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -294,9 +413,13 @@ def main():
         corr_model = learn.load_model()
     nu_gas = bp.mu0 / bp.rho0
 
+    tau = wl.tau_p()
+
     def make_step(frm, flg, with_model):
         h = pstep.ParticleStep(bp.step_config(), n, frm, flg)
         h.load(*arrs)
+        if tau is not None:
+            h.set_tau_p(tau)
         if with_model:
             h.set_correction(corr_model, nu_gas)
         h.bind_velocity(*fields[:3])
@@ -306,6 +429,8 @@ def main():
 
     g = pstep.ParticleStep(bp.step_config(), n, form, flags)
     g.load(*arrs)
+    if tau is not None:
+        g.set_tau_p(tau)
     if corr_model is not None:
         g.set_correction(corr_model, nu_gas)
     g.bind_velocity(*fields[:3])
@@ -358,12 +483,22 @@ def main():
                 "launches": dom_cnt}
     phases = {p: {"ms_per_step": v[0] / args.steps, "launch_groups": v[1]} for p, v in prof.items()}
 
+    # slip-velocity and particle-temperature statistics after warm-up + timed steps (the
+    # corrected step's report), compared below with the plain FP64 drop-in after as many
+    # steps from the same inputs
+    stats_steps = args.warmup + args.steps
+    import torch
+    u_dev = [torch.from_numpy(np.ascontiguousarray(fields[d]).ravel()).to("cuda") for d in range(3)]
+    stats_main = particle_stats(g, u_dev, bp.l, wl.n)
+
     # end to end through the C ABI with host buffers (pinned): a time-stepping loop
     # through host memory -- each step uploads the particles and fields, primes, runs
     # one step and reads back every particle array (ids included) and every deposited
     # field; the particles read back are the next step's inputs, in the order returned
     e2e = None
-    if not args.no_e2e:
+    # (per-particle tau_p would have to follow the particles' order through the host loop;
+    # the workloads that carry it are error-report workloads and skip the loop)
+    if not args.no_e2e and tau is None:
         hin = [pinned_like(a) for a in arrs]
         hout = [pinned_like(a) for a in arrs]
         hf = [pinned_like(f) for f in fields]
@@ -416,6 +551,8 @@ def main():
         ms32 = g.last_run_ms() / args.steps
         fp32_plain = {"value": world * n / (ms32 / 1e3), "ms_per_step": ms32, "form": "fp32 plain interpolation"}
     fp64 = None
+    c4_stats = None
+    fp32_error = None
     if form == pstep.FP32 and not args.no_fp64_line:
         g.close()
         g = make_step(pstep.FP64, pstep.TRACK_ORDER, False)
@@ -425,6 +562,21 @@ def main():
         g.run(args.steps)
         ms64 = g.last_run_ms() / args.steps
         fp64 = {"value": world * n / (ms64 / 1e3), "ms_per_step": ms64, "form": "fp64 drop-in (reference order)"}
+        stats64 = particle_stats(g, u_dev, bp.l, wl.n)
+        c4_stats = {"steps": stats_steps, "fields": "held fixed (the bound synthetic gas fields)",
+                    args.form: stats_main, "fp64_plain": stats64,
+                    "difference": stats_difference(stats_main, stats64)}
+    # the FP32 form's error against the FP64 step on the same inputs (one step from the
+    # inputs), for the workloads with per-particle tau_p
+    if form == pstep.FP32 and wl.tau_p_range is not None and not args.no_fp64_line:
+        g.close()
+        g = make_step(pstep.FP32, 0, False)
+        g64 = make_step(pstep.FP64, 0, False)
+        g.run(1)
+        g64.run(1)
+        fp32_error = {"steps": 1, "against": "fp64 drop-in, same inputs and per-particle tau_p",
+                      **fp32_error_report(g, g64, bp.l, wl.n)}
+        g64.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -447,6 +599,7 @@ def main():
                        "l2": "inputs larger than L2 (particle state alone is several GB)",
                        "parallelism": f"replicas x{world}", "input_generation_s": round(gen_s, 2)},
             "roofline": roof, "phases": phases, "fp32_plain": fp32_plain, "fp64_dropin": fp64, "cpu_baseline": cpu,
+            "c4_stats": c4_stats, "fp32_error": fp32_error,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clocks.summary(),

@@ -121,6 +121,14 @@ class Workload:
     dp_over_dx: float = 0.1
     mass_loading: float = 0.2
     nblobs: int = 64  # Gaussian blobs holding the clustered half of the particles (sigma 4 cells)
+    tau_p_range: tuple | None = None  # per-particle tau_p, log-uniform in [lo, hi] (None: the scalar)
+
+    def tau_p(self):
+        """The per-particle momentum relaxation times of the workload (None: scalar tau_p)."""
+        if self.tau_p_range is None:
+            return None
+        from . import gen
+        return gen.loguniform(self.seed, 31, self.n_particles, *self.tau_p_range)
 
 
 # Seeded synthetic stand-ins for the reference's run shapes.
@@ -128,6 +136,9 @@ WORKLOADS = {
     "box64_uniform": Workload("box64_uniform", 64, 1 << 15, False, 1, 1001),
     "box256_clustered": Workload("box256_clustered", 256, 1 << 24, True, 10, 1002),
     "box512_clustered": Workload("box512_clustered", 512, 1 << 27, True, 1, 1003),
+    # the mixed-precision configuration: box512_clustered's construction with tau_p
+    # log-uniform in [0.01, 1] per particle, for the FP32 form's error against FP64
+    "box512_mixed": Workload("box512_mixed", 512, 1 << 27, True, 1, 1006, tau_p_range=(0.01, 1.0)),
     # the corrected-step workload: larger, heavier particles (d_p/dx 0.5, mass loading 1.0)
     "box512_corrected": Workload("box512_corrected", 512, 1 << 27, True, 100, 1004, 0.5, 1.0),
     # box512_corrected at 1/8 of the cells and particles with 8 blobs instead of 64: each

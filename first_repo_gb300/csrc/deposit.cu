@@ -611,6 +611,24 @@ int interior_mean(pstep_ctx *h, const double *f, double *out_dev) {
   return PSTEP_OK;
 }
 
+// The momentum balance of the last int deposit: the interior sums of RHS_RU x/y/z,
+// each in the fixed order of k_sum_partial / k_sum_final (zeros without TWC).
+int momentum_sums(pstep_ctx *h) {
+  const Geom &G = h->geom;
+  if (!h->cfg.twc) {
+    PSTEP_CUDA(cudaMemsetAsync(h->mom_dev, 0, 3 * sizeof(double), h->stream));
+    return PSTEP_OK;
+  }
+  for (int d = 0; d < 3; ++d) {
+    double *part = h->red_partials + (1 + d) * kRedBlocks;
+    k_sum_partial<<<kRedBlocks, kThreads, 0, h->stream>>>(G, h->dep[PSTEP_FIELD_RU_X + d], part);
+    PSTEP_LAUNCHED(h);
+    k_sum_final<<<1, kThreads, 0, h->stream>>>(part, kRedBlocks, 1.0, h->mom_dev + d);
+    PSTEP_LAUNCHED(h);
+  }
+  return PSTEP_OK;
+}
+
 // part2gas_Temp_int/new: deposit RHS_T with the records of csr/frac/key, fold, refresh, mean.
 bool reference_sums(const pstep_ctx *h) {
   return (h->cfg.flags & PSTEP_TRACK_ORDER) && (h->cfg.flags & PSTEP_REFERENCE_SUMS);
@@ -657,11 +675,13 @@ int f64_deposit_int(pstep_ctx *h) {
     if (rc) return rc;
     if (h->cfg.twc) {
       double *ru[3] = {h->dep[PSTEP_FIELD_RU_X], h->dep[PSTEP_FIELD_RU_Y], h->dep[PSTEP_FIELD_RU_Z]};
-      return fold_fields(h, ru, 3, 1);
+      rc = fold_fields(h, ru, 3, 1);
+      if (rc) return rc;
+    } else {
+      for (int q = PSTEP_FIELD_RU_X; q <= PSTEP_FIELD_RU_Z; ++q)
+        PSTEP_CUDA(cudaMemsetAsync(h->dep[q], 0, sizeof(double) * G.gsize, h->stream));
     }
-    for (int q = PSTEP_FIELD_RU_X; q <= PSTEP_FIELD_RU_Z; ++q)
-      PSTEP_CUDA(cudaMemsetAsync(h->dep[q], 0, sizeof(double) * G.gsize, h->stream));
-    return PSTEP_OK;
+    return momentum_sums(h);
   }
   k_dep_trilinear<<<blocks_for(G.gsize), kThreads, 0, h->stream>>>(G, d, 0, h->dep[PSTEP_FIELD_C]);
   PSTEP_LAUNCHED(h);
@@ -682,7 +702,7 @@ int f64_deposit_int(pstep_ctx *h) {
     for (int q = PSTEP_FIELD_RU_X; q <= PSTEP_FIELD_RU_Z; ++q)
       PSTEP_CUDA(cudaMemsetAsync(h->dep[q], 0, sizeof(double) * G.gsize, h->stream));  // RHS_RU = 0 (grid.cpp:671)
   }
-  return PSTEP_OK;
+  return momentum_sums(h);
 }
 
 }  // namespace pstep

@@ -138,7 +138,7 @@ void release(pstep_ctx *h) {
   for (int d = 0; d < 3; ++d) dfree(h->own_u[d]);
   dfree(h->own_t);
   for (int f = 0; f < PSTEP_NUM_FIELDS; ++f) dfree(h->dep[f]);
-  dfree(h->emean_dev); dfree(h->red_partials);
+  dfree(h->emean_dev); dfree(h->mom_dev); dfree(h->red_partials);
   dfree(h->ref_of_phys); dfree(h->phys_of_ref); dfree(h->leave_code); dfree(h->ord_scratch); dfree(h->ord_count);
   dfree(h->err_word);
   if (is_f32(h)) f32_destroy(h);
@@ -195,7 +195,9 @@ int alloc_all(pstep_ctx *h) {
     PSTEP_CUDA(cudaMemsetAsync(h->dep[f], 0, sizeof(double) * gs, h->stream));
   }
   TRY(dalloc(h, h->emean_dev, 1));
-  TRY(dalloc(h, h->red_partials, 1024));
+  TRY(dalloc(h, h->mom_dev, 3));
+  PSTEP_CUDA(cudaMemsetAsync(h->mom_dev, 0, 3 * sizeof(double), h->stream));
+  TRY(dalloc(h, h->red_partials, 4 * 1024));
   TRY(dalloc(h, h->err_word, 1));
   PSTEP_CUDA(cudaMemsetAsync(h->err_word, 0, sizeof(int32_t), h->stream));
   PSTEP_CUDA(cudaMemsetAsync(h->emean_dev, 0, sizeof(double), h->stream));
@@ -622,6 +624,21 @@ int pstep_energy_mean(pstep_handle h, double *out) {
   PSTEP_CUDA(cudaMemcpyAsync(&h->emean_host, h->emean_dev, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   PSTEP_CUDA(cudaStreamSynchronize(h->stream));
   *out = h->emean_host;
+  return PSTEP_OK;
+}
+
+int pstep_set_wait_limit(pstep_handle h, uint32_t polls, int idle_first) {
+  if (!h) return PSTEP_ERR_ARG;
+  h->wait_limit = polls;
+  h->wait_idle = idle_first ? 1 : 0;
+  return PSTEP_OK;
+}
+
+int pstep_momentum_sums(pstep_handle h, double *out) {
+  if (!h || !out) return PSTEP_ERR_ARG;
+  PSTEP_CUDA(cudaMemcpyAsync(h->mom_host, h->mom_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+  for (int d = 0; d < 3; ++d) out[d] = h->mom_host[d];
   return PSTEP_OK;
 }
 

@@ -79,6 +79,8 @@ struct pstep_ctx {
   int64_t cap;
   int num_sms;
   int corr_on;                              // learned correction active (FP32 form)
+  uint32_t wait_limit;                      // polls of the tensor-core completion waits (0: default)
+  int wait_idle;                            // timeout test: first wait polls a barrier nothing signals
   alignas(16) unsigned char corr_dev[256];  // its kernel constants (stage_f32.cu)
 
   // FP64 state
@@ -104,8 +106,10 @@ struct pstep_ctx {
   double *own_u[3], *own_t;
   double *dep[PSTEP_NUM_FIELDS];
   double *emean_dev;       // device scalar
-  double *red_partials;    // reduction scratch
+  double *mom_dev;         // device: interior sums of the three deposited momentum fields (last stage)
+  double *red_partials;    // reduction scratch (4 x 1024)
   double emean_host;
+  double mom_host[3];
 
   // reference-order bookkeeping
   int32_t *ref_of_phys, *phys_of_ref;
@@ -175,6 +179,7 @@ __global__ void k_gather(const T *__restrict__ src, const int32_t *__restrict__ 
 int fold_cum(pstep_ctx *h, double *f);
 int refresh_ghosts(pstep_ctx *h, double *f);
 int interior_mean(pstep_ctx *h, const double *f, double *out_dev);
+int momentum_sums(pstep_ctx *h);
 int order_passes(pstep_ctx *h);
 int order_init(pstep_ctx *h);
 int order_permute(pstep_ctx *h, const int32_t *sidx);

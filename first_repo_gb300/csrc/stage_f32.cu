@@ -106,6 +106,7 @@ struct F32Form {
   uint32_t *bounds;   // [0..2] max |RHS_u| per component (float bits), [3] max |RHS_T|, [4] max per-cell count
   uint32_t *slots;    // kBoundSlots x 4 partial maxima (spread so blocks do not contend on one word)
   int32_t *se;        // fixed-point scale exponents per field
+  unsigned long long *totals;  // exact integer totals of the five fields of the last deposit
   Work work;
   int launch_no;      // deposit launches since the last work-list build (counter index)
   void *corr_mem;     // learned correction: packed weight image + biases (device), or nullptr
@@ -269,6 +270,19 @@ __device__ __forceinline__ float adv_finish_t(const Geom &G, const F32Form &f, c
       in_[d] = ia[d];
     }
   }
+  // x_new within one cell of the step-start cell on every axis: the deposit's source
+  // windows (two cells around a brick) hold a particle's x_int and x_new cells only then
+  {
+    bool far = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int r = in_[d] - ib[d];
+      r += (r < -(G.n[d] >> 1)) ? G.n[d] : 0;
+      r -= (r > (G.n[d] >> 1)) ? G.n[d] : 0;
+      far |= (r < -1 || r > 1);
+    }
+    if (far) atomicOr(err, kErrMove);
+  }
   // velocity and temperature (particle.cpp:362-399, 480-496)
   float rhs[3], vn[4];
 #pragma unroll
@@ -376,13 +390,15 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
 namespace corr {
 constexpr int kRows = 128, kInP = 16, kHid = 64, kOutP = 16, kGroups = 2, kThreads = kRows * kGroups;
 // shared memory: weight image W1 | W2 | W3 (bf16 tiles), biases, then per warpgroup
-// X [128 x 16], H [128 x 64] (layer 1, then layer 2 output) and its mbarrier
+// X [128 x 16], H [128 x 64] (layer 1, then layer 2 output), its MMA mbarrier and an
+// idle mbarrier that nothing signals (the wait-timeout test, pstep_set_wait_limit)
 constexpr uint32_t W1 = 0, W2 = W1 + kHid * kInP * 2, W3 = W2 + kHid * kHid * 2, kImage = W3 + kOutP * kHid * 2;
 constexpr uint32_t BIAS = kImage, GROUPS = 13 * 1024;
-constexpr uint32_t G_XA = 0, G_H = G_XA + kRows * kInP * 2, G_BAR = G_H + kRows * kHid * 2, kGroupStride = 21 * 1024;
+constexpr uint32_t G_XA = 0, G_H = G_XA + kRows * kInP * 2, G_BAR = G_H + kRows * kHid * 2, G_IDLE = G_BAR + 8,
+                   kGroupStride = 21 * 1024;
 constexpr uint32_t TSLOT = GROUPS + kGroups * kGroupStride, kBytes = TSLOT + 16;
 static_assert(BIAS + (kHid + kHid + kOutP) * 4 <= GROUPS, "correction smem");
-static_assert(G_BAR + 8 <= kGroupStride, "correction group smem");
+static_assert(G_IDLE + 8 <= kGroupStride, "correction group smem");
 // with this much shared memory at most 4 CTAs fit on an SM (228 KB), so their
 // 4 x 128 tensor-memory columns never exceed the 512 an SM has and no allocation waits
 constexpr uint32_t kAlloc = kBytes;
@@ -399,6 +415,9 @@ struct CorrDev {
   float dp_per_itth;   // d_p = itth * dp_per_itth (1 / (Nu PI k)), per-particle diameters
   float dp;            // scalar diameter (no per-particle itth)
   float idx;           // 1 / dx
+  uint32_t wait_limit; // polls of each MMA completion wait (the drain before freeing tensor memory
+                       // always allows corr::kWaitLimit)
+  uint32_t idle_first; // 1: each warpgroup's first completion wait polls the idle barrier (test)
 };
 
 static_assert(sizeof(CorrDev) <= sizeof(((pstep_ctx *)nullptr)->corr_dev), "correction constants");
@@ -438,8 +457,8 @@ __device__ __forceinline__ void group_sync_mma(int wg) {
   group_bar(wg);
   tc05::fence_after();
 }
-__device__ __forceinline__ bool group_wait(int wg, uint64_t *mbar, uint32_t &phase) {
-  const bool ok = tc05::mbar_wait(mbar, phase, corr::kWaitLimit);
+__device__ __forceinline__ bool group_wait(int wg, uint64_t *mbar, uint32_t &phase, uint32_t limit) {
+  const bool ok = tc05::mbar_wait(mbar, phase, limit);
   tc05::fence_after();
   const bool all = group_and(wg, ok);
   if (all) phase ^= 1u;
@@ -508,12 +527,17 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
   uint8_t *gbase = sm + corr::GROUPS + wg * corr::kGroupStride;
   uint8_t *XA = gbase + corr::G_XA, *H = gbase + corr::G_H;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(gbase + corr::G_BAR);
+  uint64_t *idle = reinterpret_cast<uint64_t *>(gbase + corr::G_IDLE);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + corr::TSLOT);
+  const uint32_t limit = cd.wait_limit ? cd.wait_limit : corr::kWaitLimit;
   for (uint32_t q = tid; q < corr::kImage / 16; q += corr::kThreads) reinterpret_cast<uint4 *>(sm)[q] = cd.image[q];
   // hidden-layer biases halved for silu_half (exact: a power-of-two scale)
   for (int q = tid; q < corr::kHid + corr::kHid + corr::kOutP; q += corr::kThreads)
     b1[q] = q < 2 * corr::kHid ? 0.5f * cd.bias[q] : cd.bias[q];
-  if (lt == 0) mbar_init(mbar, 1);
+  if (lt == 0) {
+    mbar_init(mbar, 1);
+    mbar_init(idle, 1);
+  }
   if (warp == 0) tmem_alloc(tslot, 128);
   tc05::fence_smem_async();
   tc05::fence_before();
@@ -525,6 +549,7 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
   const uint32_t sX = smem_u32(XA), sH = smem_u32(H), sW1 = smem_u32(W1), sW2 = smem_u32(W2), sW3 = smem_u32(W3);
   uint32_t phase = 0;
   bool ok = true;
+  bool first = cd.idle_first != 0;
   float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
   const int64_t ntiles = (n + corr::kRows - 1) / corr::kRows;
   for (int64_t tile = (int64_t)blockIdx.x * corr::kGroups + wg; tile < ntiles && ok;
@@ -579,7 +604,10 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
       mma_bf16(tcol, tile_desc(sX, corr::kInP, 0, 0), tile_desc(sW1, corr::kInP, 0, 0), id64, 0);
       commit(mbar);
     }
-    ok = group_wait(wg, mbar, phase);
+    // (the timeout test polls the idle barrier here, as a completion that never arrives;
+    // the MMA's own completion is then drained below before the tensor memory is freed)
+    ok = group_wait(wg, first ? idle : mbar, phase, limit);
+    first = false;
     if (!ok) break;
 #pragma unroll
     for (int cc = 0; cc < 4; ++cc) {
@@ -594,7 +622,7 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
         mma_bf16(tcol, tile_desc(sH, corr::kHid, 0, ks), tile_desc(sW2, corr::kHid, 0, ks), id64, ks);
       commit(mbar);
     }
-    ok = group_wait(wg, mbar, phase);
+    ok = group_wait(wg, mbar, phase, limit);
     if (!ok) break;
 #pragma unroll
     for (int cc = 0; cc < 4; ++cc) {  // layer 2 output overwrites layer 1's in H (its MMA is done)
@@ -609,7 +637,7 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
         mma_bf16(tcol, tile_desc(sH, corr::kHid, 0, ks), tile_desc(sW3, corr::kHid, 0, ks), id16, ks);
       commit(mbar);
     }
-    ok = group_wait(wg, mbar, phase);
+    ok = group_wait(wg, mbar, phase, limit);
     if (!ok) break;
     float y[16];
     tmem_ld16(tl, y);
@@ -783,21 +811,24 @@ __device__ inline int rel_local(int c, int b, int n) {
 // most kChunkMax = 2^16 particles. The sum is hi * 2^16 + lo, exact whatever the
 // order of the adds.
 constexpr int32_t kChunkMax = 1 << 16;
-// Contributions outside the brick (pred false) go to the lane's own sink words
-// (never read), so the adds are branch-free.
-__device__ __forceinline__ void add_fixed32(uint32_t *lo, uint32_t *hi, int32_t v, bool pred, uint32_t *sink) {
-  atomicAdd(pred ? lo : sink, (uint32_t)v & 0xffffu);
-  atomicAdd(pred ? hi : sink + 32, (uint32_t)(v >> 16));
+__device__ __forceinline__ void add_fixed32(uint32_t *lo, uint32_t *hi, int32_t v) {
+  atomicAdd(lo, (uint32_t)v & 0xffffu);
+  atomicAdd(hi, (uint32_t)(v >> 16));
 }
 __device__ __forceinline__ long long get_fixed(const uint32_t *lo, const uint32_t *hi) {
   return (long long)(int32_t)*hi * 65536ll + (long long)*lo;
 }
 
-// accumulator slot of brick-local cell (x,y,z): rows padded by one word so that
-// neighbouring rows do not fall on the same shared-memory banks
+// Accumulator of a deposit brick: its BR^3 cells and one cell around them,
+// brick-relative x, y, z in [-1, BR], rows padded by one word so that neighbouring
+// rows do not fall on the same shared-memory banks. A particle whose every target
+// lies in this region adds without a per-target test; what lands in the outer
+// layer is not read (the neighbouring brick counts it for its own cells).
 template <int BR> struct Acc {
-  static constexpr int kRow = BR + 1, kSlots = kRow * BR * BR;
-  static __device__ __forceinline__ int slot(int x, int y, int z) { return (z * BR + y) * kRow + x; }
+  static constexpr int kSide = BR + 2, kRow = BR + 3, kSlots = kRow * kSide * kSide;
+  static __device__ __forceinline__ int slot(int x, int y, int z) {
+    return ((z + 1) * kSide + (y + 1)) * kRow + (x + 1);
+  }
 };
 
 // The source window of the deposit brick at (bx, by, bz) -- its cells and two
@@ -869,57 +900,47 @@ __global__ void k_work_fill(Work w, int nb) {
   }
 }
 
-// trilinear deposit (particle.cpp:526-559, :586-658) of a particle at brick-relative cell r3
-// with in-cell offsets o3 and value `val` (already times the field's fixed-point scale):
-// node = cell + h, the 8 cells node - 1 .. node get products of x_l / (1 - x_l)
+// trilinear deposit (particle.cpp:526-559, :586-658) of a particle with in-cell offsets
+// o3 whose round() node is `node` (brick-relative, each axis in [0, BR]) and value `val`
+// (already times the field's fixed-point scale): the 8 cells node - 1 .. node get
+// products of x_l / (1 - x_l), all inside the accumulator region
 template <int BR>
-__device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, const int r3[3], const float o3[3],
-                                                  float val, uint32_t *sink) {
+__device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, const int node[3], const float o3[3],
+                                                  float val) {
   float w[3][2];
-  int t0[3];
-  bool ok[3][2];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int hh = o3[d] >= 0.5f;
-    const float xl = o3[d] - hh + 0.5f;
-    t0[d] = r3[d] + hh - 1;  // target of the "1 - x_l" side; t0 + 1 gets x_l
-    w[d][0] = 1.f - xl;
-    w[d][1] = xl;
-    ok[d][0] = (unsigned)t0[d] < (unsigned)BR;
-    ok[d][1] = (unsigned)(t0[d] + 1) < (unsigned)BR;
+    const float xl = o3[d] - (o3[d] >= 0.5f ? 1.f : 0.f) + 0.5f;
+    w[d][0] = 1.f - xl;  // cell node - 1
+    w[d][1] = xl;        // cell node
   }
-  const int base = Acc<BR>::slot(t0[0], t0[1], t0[2]);
+  const int base = Acc<BR>::slot(node[0] - 1, node[1] - 1, node[2] - 1);
 #pragma unroll
   for (int oz = 0; oz < 2; ++oz)
 #pragma unroll
     for (int oy = 0; oy < 2; ++oy) {
       const float wyz = w[2][oz] * w[1][oy] * val;
-      const bool pyz = ok[2][oz] && ok[1][oy];
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) {
-        const int sl = base + (oz * BR + oy) * Acc<BR>::kRow + ox;
-        add_fixed32(lo + sl, hi + sl, __float2int_rn(w[0][ox] * wyz), pyz && ok[0][ox], sink);
+        const int sl = base + (oz * Acc<BR>::kSide + oy) * Acc<BR>::kRow + ox;
+        add_fixed32(lo + sl, hi + sl, __float2int_rn(w[0][ox] * wyz));
       }
     }
 }
 
-// face-normal deposits (particle.cpp:498-524): along d, face r3[d] gets (1 - x_l) R_d and
-// face r3[d] + 1 gets x_l R_d, at the particle's cell across. lo[d]/hi[d]: field d's words.
+// face-normal deposits (particle.cpp:498-524) of a particle in brick-relative cell r3
+// (each axis in [-1, BR - 1]): along d, face r3[d] gets (1 - x_l) R_d and face
+// r3[d] + 1 gets x_l R_d, at the particle's cell across. lo[d]/hi[d]: field d's words.
 template <int BR>
 __device__ __forceinline__ void deposit_faces(uint32_t *const *lo, uint32_t *const *hi, const int r3[3],
-                                              const float o3[3], const float ru[3], const float *scale,
-                                              uint32_t *sink) {
-  const bool in0 = (unsigned)r3[0] < (unsigned)BR, in1 = (unsigned)r3[1] < (unsigned)BR,
-             in2 = (unsigned)r3[2] < (unsigned)BR;
-  const bool acr[3] = {in1 && in2, in0 && in2, in0 && in1};
+                                              const float o3[3], const float ru[3], const float *scale) {
   const int sl0 = Acc<BR>::slot(r3[0], r3[1], r3[2]);
-  const int step[3] = {1, Acc<BR>::kRow, BR * Acc<BR>::kRow};
+  constexpr int step[3] = {1, Acc<BR>::kRow, Acc<BR>::kSide * Acc<BR>::kRow};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float r = ru[d] * scale[1 + d];
-    const bool lo_in = (unsigned)r3[d] < (unsigned)BR, hi_in = (unsigned)(r3[d] + 1) < (unsigned)BR;
-    add_fixed32(lo[d] + sl0, hi[d] + sl0, __float2int_rn((1.f - o3[d]) * r), acr[d] && lo_in, sink);
-    add_fixed32(lo[d] + sl0 + step[d], hi[d] + sl0 + step[d], __float2int_rn(o3[d] * r), acr[d] && hi_in, sink);
+    add_fixed32(lo[d] + sl0, hi[d] + sl0, __float2int_rn((1.f - o3[d]) * r));
+    add_fixed32(lo[d] + sl0 + step[d], hi[d] + sl0 + step[d], __float2int_rn(o3[d] * r));
   }
 }
 
@@ -954,41 +975,64 @@ __device__ __forceinline__ void block_exclusive_scan2(int32_t *a, int n, int32_t
   __syncthreads();
 }
 
-// Shared memory of the deposit CTA for brick edge BR.
+// Shared memory of the deposit CTA for brick edge BR: the accumulator of the widest
+// pass (NF fields, two words per slot; a multiple of 8 bytes), block-reduction
+// scratch (32 int64), the window's row-segment prefix and starts, misc words.
 template <int BR, int NF> struct DepSmem {
   static constexpr int kRanges = Window<BR>::kRanges;
   static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR>::kSlots;
-  static constexpr size_t kBytes = 2 * kAcc + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * (40 + 64);
+  static constexpr size_t kBytes =
+      2 * kAcc + sizeof(long long) * 32 + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
   static_assert(kRanges <= 2 * DepTraits<BR>::kThreads, "ranges exceed the block scan");
 };
 
-// Deposit into bricks of BR^3 interior cells, one walk over each brick's source
-// particles per stage: at the *_int positions the concentration and the face
-// momentum (DO_INT), at the *_new positions RHS_T (DO_NEW). Field slots:
-// 0 C, 1-3 RHS_RU x/y/z, 4 RHS_Part_Temp (scale exponents f.se[0..4]).
-// Each thread finds its particles' row segments from the segments' prefix counts.
+// block sum of one int64 per thread; every thread calls it, thread 0 gets the result
+__device__ __forceinline__ long long block_sum_i64(long long v, long long *scratch) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+  __syncthreads();  // the scratch may still be read by a previous call
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  long long s = 0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < nw; ++q) s += scratch[q];  // fixed order (integer: exact anyway)
+  return s;
+}
+
+// Deposit into bricks of BR^3 interior cells. A work item walks its brick's source
+// window (the particles whose step-start cell lies within two cells of the brick)
+// once per pass:
+//   pass A (DO_INT): the concentration and the face momentum at the *_int positions
+//     (fields C, RHS_RU x/y/z); a particle counts when its x_int cell lies within one
+//     cell of the brick -- its trilinear node in [0, BR] and, for the faces, its cell
+//     in [-1, BR - 1] -- and then adds every target without a test;
+//   pass B (DO_NEW): RHS_T at the *_new positions (RHS_Part_Temp), the same way.
+// Scale exponents f.se[0..4]. Each brick's exact integer field totals are added to
+// `totals` (five int64 words, zeroed before the launch): the momentum and energy
+// balance sums, exact and independent of the order of the work.
 template <bool DO_INT, bool DO_NEW, int BR>
 __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w,
                                                                    int twc, double *__restrict__ outC,
                                                                    double *__restrict__ outX,
                                                                    double *__restrict__ outY,
                                                                    double *__restrict__ outZ,
-                                                                   double *__restrict__ outE) {
-  constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
-  constexpr int FE = DO_INT ? 4 : 0;  // accumulator index of RHS_Part_Temp
+                                                                   double *__restrict__ outE,
+                                                                   unsigned long long *__restrict__ totals) {
+  constexpr int NF = DO_INT ? 4 : 1;  // fields of the widest pass
   constexpr int NB3 = BR * BR * BR;
   constexpr int SLOTS = Acc<BR>::kSlots;
   constexpr int NR = Window<BR>::kRanges;
   extern __shared__ __align__(16) uint8_t dsm[];
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(dsm);
   uint32_t *acc_hi = acc_lo + NF * SLOTS;
-  int32_t *pre = reinterpret_cast<int32_t *>(acc_hi + NF * SLOTS);  // NR + 1
-  int32_t *beg = pre + NR + 1;                                       // NR
-  int32_t *misc = beg + NR;                                          // 32 warp sums, item, last
-  uint32_t *sink = reinterpret_cast<uint32_t *>(misc + 40) + (threadIdx.x & 31);  // 2 x 32 words
-  uint32_t *lo_f[5], *hi_f[5];
+  long long *red = reinterpret_cast<long long *>(acc_hi + NF * SLOTS);  // 32 (8-byte aligned)
+  int32_t *pre = reinterpret_cast<int32_t *>(red + 32);                 // NR + 1
+  int32_t *beg = pre + NR + 1;                                          // NR
+  int32_t *misc = beg + NR;                                             // 32 warp sums, item, last
+  uint32_t *lo_f[4], *hi_f[4];
 #pragma unroll
-  for (int q = 0; q < 5; ++q) {
+  for (int q = 0; q < 4; ++q) {
     lo_f[q] = acc_lo + (q < NF ? q : 0) * SLOTS;
     hi_f[q] = acc_hi + (q < NF ? q : 0) * SLOTS;
   }
@@ -1009,10 +1053,8 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     const int nch = w.nchunk[brick];
     const int bx = (brick % ndx) * BR, by = ((brick / ndx) % ndy) * BR, bz = (brick / (ndx * ndy)) * BR;
     const int b3[3] = {bx, by, bz};
-    for (int s = threadIdx.x; s < NF * SLOTS; s += blockDim.x) {
-      acc_lo[s] = 0u;
-      acc_hi[s] = 0u;
-    }
+    const int slot_idx = nch > 1 ? w.slot[brick] : -1;
+    long long *tile = slot_idx >= 0 ? w.tiles + (int64_t)slot_idx * 5 * NB3 : nullptr;
     for (int r = threadIdx.x; r < NR; r += blockDim.x) {
       uint32_t id;
       int len;
@@ -1037,86 +1079,138 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     const int32_t g1 = t0 + (int32_t)(((int64_t)(t1 - t0) * (grp + 1)) / ngroups);
     // segment of the thread's first particle: the last r with pre[r] <= t (binary
     // search); later particles only move forward (pre[NR] = total > t ends the scan)
-    int seg = 0;
+    int seg0 = 0;
     {
       const int32_t tf = g0 + (int32_t)(threadIdx.x & 7);
       int hi = NR;
-      while (hi - seg > 1) {
-        const int mid = (seg + hi) >> 1;
-        if (pre[mid] <= tf) seg = mid; else hi = mid;
+      while (hi - seg0 > 1) {
+        const int mid = (seg0 + hi) >> 1;
+        if (pre[mid] <= tf) seg0 = mid; else hi = mid;
       }
     }
-    for (int32_t t = g0 + (int32_t)(threadIdx.x & 7); t < g1; t += 8) {
-      while (pre[seg + 1] <= t) ++seg;
-      const int32_t p = beg[seg] + (t - pre[seg]);
-      if (DO_INT) {
-        const uint32_t c = SI.cell[p];
+#pragma unroll 1
+    for (int pass = DO_INT ? 0 : 1; pass <= (DO_NEW ? 1 : 0); ++pass) {
+      const int nf = pass == 0 ? 4 : 1;  // accumulated fields of this pass
+      for (int s = threadIdx.x; s < nf * SLOTS; s += blockDim.x) {
+        acc_lo[s] = 0u;
+        acc_hi[s] = 0u;
+      }
+      __syncthreads();
+      int seg = seg0;
+      const uint32_t *__restrict__ cellp = pass == 0 ? SI.cell : SN.cell;
+      const float *__restrict__ op0 = pass == 0 ? SI.o[0] : SN.o[0];
+      const float *__restrict__ op1 = pass == 0 ? SI.o[1] : SN.o[1];
+      const float *__restrict__ op2 = pass == 0 ? SI.o[2] : SN.o[2];
+      for (int32_t t = g0 + (int32_t)(threadIdx.x & 7); t < g1; t += 8) {
+        while (pre[seg + 1] <= t) ++seg;
+        const int32_t p = beg[seg] + (t - pre[seg]);
+        const uint32_t c = cellp[p];
         int r3[3];
         r3[0] = rel_local(ci_(c), b3[0], G.n[0]);
         r3[1] = rel_local(cj_(c), b3[1], G.n[1]);
         r3[2] = rel_local(ck_(c), b3[2], G.n[2]);
-        // reachable targets: trilinear cells r3 - 1 .. r3 + 1, faces r3 .. r3 + 1 (normal) and r3 (across)
-        if (r3[0] >= -1 && r3[0] <= BR && r3[1] >= -1 && r3[1] <= BR && r3[2] >= -1 && r3[2] <= BR) {
-          const float o3[3] = {SI.o[0][p], SI.o[1][p], SI.o[2][p]};
-          deposit_trilinear<BR>(lo_f[0], hi_f[0], r3, o3, scale[0], sink);
-          if (twc) {
+        // only a cell within one of the brick ([-1, BR] per axis) reaches it; then every
+        // target of the particle lies in the accumulator
+        if ((unsigned)(r3[0] + 1) > (unsigned)(BR + 1) || (unsigned)(r3[1] + 1) > (unsigned)(BR + 1) ||
+            (unsigned)(r3[2] + 1) > (unsigned)(BR + 1))
+          continue;
+        const float o3[3] = {op0[p], op1[p], op2[p]};
+        const int node[3] = {r3[0] + (o3[0] >= 0.5f ? 1 : 0), r3[1] + (o3[1] >= 0.5f ? 1 : 0),
+                             r3[2] + (o3[2] >= 0.5f ? 1 : 0)};
+        // trilinear targets node - 1 .. node meet the brick iff the node is in [0, BR]
+        const bool tri = (unsigned)node[0] <= (unsigned)BR && (unsigned)node[1] <= (unsigned)BR &&
+                         (unsigned)node[2] <= (unsigned)BR;
+        if (pass == 0) {
+          if (tri) deposit_trilinear<BR>(lo_f[0], hi_f[0], node, o3, scale[0]);
+          // faces r3 .. r3 + 1 along d, r3 across, meet the brick iff r3 is in [-1, BR - 1]
+          if (twc && r3[0] < BR && r3[1] < BR && r3[2] < BR) {
             const float ru[3] = {f.rhs_u[0][p], f.rhs_u[1][p], f.rhs_u[2][p]};
-            deposit_faces<BR>(&lo_f[1], &hi_f[1], r3, o3, ru, scale, sink);
+            deposit_faces<BR>(&lo_f[1], &hi_f[1], r3, o3, ru, scale);
+          }
+        } else if (tri) {
+          deposit_trilinear<BR>(lo_f[0], hi_f[0], node, o3, f.rhs_t[p] * scale[4]);
+        }
+      }
+      __syncthreads();
+      // this pass's fields: into the split brick's global tile, or written out
+      const int fbase = pass == 0 ? 0 : 4;
+      if (tile) {
+        for (int s = threadIdx.x; s < nf * NB3; s += blockDim.x) {
+          const int q = s / NB3, r = s % NB3;
+          const int sl = q * SLOTS + Acc<BR>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
+          const long long v = get_fixed(&acc_lo[sl], &acc_hi[sl]);
+          if (v) atomicAdd((unsigned long long *)&tile[(fbase + q) * NB3 + r], (unsigned long long)v);
+        }
+      } else {
+        long long tot[4] = {0, 0, 0, 0};
+        double *const dst[4] = {pass == 0 ? outC : outE, outX, outY, outZ};
+        int se[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) se[q] = f.se[pass == 0 ? q : 4];
+        const bool zero_ru = pass == 0 && !twc;  // RHS_RU = 0 without TWC (grid.cpp:671)
+        for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
+          const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
+          const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
+          const int sl = Acc<BR>::slot(lx, ly, lz);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (q >= nf) break;
+            const long long v = get_fixed(&lo_f[q][sl], &hi_f[q][sl]);
+            const bool z = q >= 1 && zero_ru;
+            dst[q][g] = z ? 0.0 : fixed_to_f64(v, se[q]);
+            tot[q] += z ? 0 : v;
           }
         }
-      }
-      if (DO_NEW) {
-        const uint32_t c = SN.cell[p];
-        int r3[3];
-        r3[0] = rel_local(ci_(c), b3[0], G.n[0]);
-        r3[1] = rel_local(cj_(c), b3[1], G.n[1]);
-        r3[2] = rel_local(ck_(c), b3[2], G.n[2]);
-        if (r3[0] >= -1 && r3[0] <= BR && r3[1] >= -1 && r3[1] <= BR && r3[2] >= -1 && r3[2] <= BR) {
-          const float o3[3] = {SN.o[0][p], SN.o[1][p], SN.o[2][p]};
-          deposit_trilinear<BR>(lo_f[FE], hi_f[FE], r3, o3, f.rhs_t[p] * scale[4], sink);
+        for (int q = 0; q < nf; ++q) {
+          const long long s = block_sum_i64(tot[q], red);
+          if (threadIdx.x == 0 && s) atomicAdd(&totals[fbase + q], (unsigned long long)s);
         }
       }
+      __syncthreads();  // the accumulator is read before the next pass clears it
     }
-    __syncthreads();
-    const int slot = nch > 1 ? w.slot[brick] : -1;
-    long long *tile = slot >= 0 ? w.tiles + (int64_t)slot * 5 * NB3 : nullptr;
     if (tile) {
-      // split brick: add this slice into the brick's global tile; the last slice writes the cells
-      for (int s = threadIdx.x; s < NF * NB3; s += blockDim.x) {
-        const int q = s / NB3, r = s % NB3;
-        const int sl = q * SLOTS + Acc<BR>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
-        const long long v = get_fixed(&acc_lo[sl], &acc_hi[sl]);
-        if (v) atomicAdd((unsigned long long *)&tile[s], (unsigned long long)v);
-      }
+      // split brick: the last slice writes the cells from the tile
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) misc[33] = (atomicAdd(&w.done[slot], 1) == nch - 1);
+      if (threadIdx.x == 0) misc[33] = (atomicAdd(&w.done[slot_idx], 1) == nch - 1);
       __syncthreads();
       const int last = misc[33];
-      if (!last) continue;
-      __threadfence();
-    }
-    for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
-      const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
-      const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
-      const int sl = Acc<BR>::slot(lx, ly, lz);
+      if (last) {
+        __threadfence();
+        long long tot[5] = {0, 0, 0, 0, 0};
+        for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
+          const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
+          const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
 #pragma unroll
-      for (int fld = 0; fld < 5; ++fld) {
-        if (fld < 4 ? !DO_INT : !DO_NEW) continue;
-        const int q = fld < 4 ? fld : FE;
-        long long v;
-        if (tile) {
-          v = __ldcg(&tile[q * NB3 + s]);
-          tile[q * NB3 + s] = 0;  // ready for the next launch
-        } else {
-          v = get_fixed(&lo_f[q][sl], &hi_f[q][sl]);
+          for (int fld = 0; fld < 5; ++fld) {
+            if (fld < 4 ? !DO_INT : !DO_NEW) continue;
+            const long long v = __ldcg(&tile[fld * NB3 + s]);
+            tile[fld * NB3 + s] = 0;  // ready for the next launch
+            const bool zero_ru = fld >= 1 && fld <= 3 && !twc;
+            outs[fld][g] = zero_ru ? 0.0 : fixed_to_f64(v, f.se[fld]);
+            tot[fld] += zero_ru ? 0 : v;
+          }
         }
-        outs[fld][g] = (fld >= 1 && fld <= 3 && !twc) ? 0.0 : fixed_to_f64(v, f.se[fld]);
+        for (int fld = 0; fld < 5; ++fld) {
+          if (fld < 4 ? !DO_INT : !DO_NEW) continue;
+          const long long s = block_sum_i64(tot[fld], red);
+          if (threadIdx.x == 0 && s) atomicAdd(&totals[fld], (unsigned long long)s);
+        }
+        if (threadIdx.x == 0) w.done[slot_idx] = 0;
       }
+      __syncthreads();
     }
-    if (tile && threadIdx.x == 0) w.done[slot] = 0;
-    __syncthreads();
   }
+}
+
+// the balance sums of the last deposit: the exact integer field totals as fp64
+// (correctly rounded), momentum components summed and the energy as the interior mean
+__global__ void k_totals(F32Form f, const unsigned long long *__restrict__ totals, int do_int, int do_new,
+                         double inv_cells, double *__restrict__ mom, double *__restrict__ emean) {
+  if (threadIdx.x != 0) return;
+  if (do_int)
+    for (int d = 0; d < 3; ++d) mom[d] = fixed_to_f64((long long)totals[1 + d], f.se[1 + d]);
+  if (do_new) *emean = fixed_to_f64((long long)totals[4], f.se[4]) * inv_cells;
 }
 
 __global__ void k_to_f32(const double *__restrict__ src, int64_t n, double shift, float *__restrict__ dst) {
@@ -1378,9 +1472,18 @@ int f32_create(pstep_ctx *h) {
     TRY32(dalloc32(h, f->set[s].cell, cap));
     for (int d = 0; d < 3; ++d) TRY32(dalloc32(h, f->set[s].o[d], cap));
     for (int q = 0; q < 4; ++q) TRY32(dalloc32(h, f->set[s].v[q], cap));
+    // zeros (cell 0, offset 0) until a stage writes them: a stage that stopped early
+    // (a device-side error) leaves nothing unwritten behind it
+    PSTEP_CUDA(cudaMemsetAsync(f->set[s].cell, 0, sizeof(uint32_t) * cap, h->stream));
+    for (int d = 0; d < 3; ++d) PSTEP_CUDA(cudaMemsetAsync(f->set[s].o[d], 0, sizeof(float) * cap, h->stream));
+    for (int q = 0; q < 4; ++q) PSTEP_CUDA(cudaMemsetAsync(f->set[s].v[q], 0, sizeof(float) * cap, h->stream));
   }
   TRY32(dalloc32(h, f->rhs_t, cap));
-  for (int d = 0; d < 3; ++d) TRY32(dalloc32(h, f->rhs_u[d], cap));
+  PSTEP_CUDA(cudaMemsetAsync(f->rhs_t, 0, sizeof(float) * cap, h->stream));
+  for (int d = 0; d < 3; ++d) {
+    TRY32(dalloc32(h, f->rhs_u[d], cap));
+    PSTEP_CUDA(cudaMemsetAsync(f->rhs_u[d], 0, sizeof(float) * cap, h->stream));
+  }
   if (h->cfg.flags & PSTEP_KEEP_GAS)
     for (int q = 0; q < 4; ++q) {
       TRY32(dalloc32(h, f->gas[q], cap));
@@ -1425,6 +1528,7 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->slots, kBoundSlots * 4));
   PSTEP_CUDA(cudaMemsetAsync(f->slots, 0, kBoundSlots * 4 * sizeof(uint32_t), h->stream));
   TRY32(dalloc32(h, f->se, 8));
+  TRY32(dalloc32(h, f->totals, 8));
   TRY32(dalloc32(h, h->s.flag, cap));
   PSTEP_CUDA(cudaMemsetAsync(f->bounds, 0, 8 * sizeof(uint32_t), h->stream));
   return PSTEP_OK;
@@ -1446,7 +1550,7 @@ int f32_destroy(pstep_ctx *h) {
   dfree32(f->corr_y);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx);
-  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots);
+  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots); dfree32(f->totals);
   {
     Work &w = f->work;
     dfree32(w.items); dfree32(w.nchunk); dfree32(w.slot); dfree32(w.cnt_a); dfree32(w.cnt_b); dfree32(w.cnt_s);
@@ -1710,7 +1814,9 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
   const int64_t n = h->np;
   prof_begin(h, PSTEP_PHASE_ADVANCE);
   if (n > 0 && h->corr_on) {
-    const CorrDev &cd = *reinterpret_cast<const CorrDev *>(h->corr_dev);
+    CorrDev cd = *reinterpret_cast<const CorrDev *>(h->corr_dev);
+    cd.wait_limit = h->wait_limit;
+    cd.idle_first = h->wait_idle ? 1u : 0u;
     if (k == 0) {
       // the network: persistent CTAs of two warpgroups, 3 per SM, tiles of 128 particles
       const int64_t pairs = (n + 2 * corr::kRows - 1) / (2 * corr::kRows);
@@ -1750,7 +1856,7 @@ namespace {
 // persistent CTAs (as many as fit on the SMs) pulling work items
 template <bool DO_INT, bool DO_NEW, int BR>
 int dep_run1(pstep_ctx *h, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z, double *E) {
-  constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
+  constexpr int NF = DO_INT ? 4 : 1;  // fields of the widest pass
   constexpr size_t smem = DepSmem<BR, NF>::kBytes;
   auto kern = k_dep32<DO_INT, DO_NEW, BR>;
   PSTEP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1762,7 +1868,7 @@ int dep_run1(pstep_ctx *h, Set32 SI, Set32 SN, double *C, double *X, double *Y, 
   }
   F32Form &f = *h->f32;
   kern<<<h->num_sms * per_sm, DepTraits<BR>::kThreads, smem, h->stream>>>(h->geom, f, SI, SN, f.work, h->cfg.twc,
-                                                                           C, X, Y, Z, E);
+                                                                           C, X, Y, Z, E, f.totals);
   PSTEP_LAUNCHED(h);
   return PSTEP_OK;
 }
@@ -1780,6 +1886,7 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   k_scales<<<1, 32, 0, h->stream>>>(f);  // fold this advance's maxima into the fixed-point scales
   PSTEP_LAUNCHED(h);
   PSTEP_CUDA(cudaMemsetAsync(f.work.next, 0, sizeof(int32_t), h->stream));
+  PSTEP_CUDA(cudaMemsetAsync(f.totals, 0, 5 * sizeof(unsigned long long), h->stream));
   double *C = h->dep[PSTEP_FIELD_C], *X = h->dep[PSTEP_FIELD_RU_X], *Y = h->dep[PSTEP_FIELD_RU_Y],
          *Z = h->dep[PSTEP_FIELD_RU_Z], *E = h->dep[PSTEP_FIELD_PART_TEMP];
   if (f.work.br == 16) {
@@ -1795,8 +1902,13 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   if (do_new) {
     double *e[1] = {E};
     TRY32(fold_fields(h, e, 1, 2));
-    return interior_mean(h, E, h->emean_dev);
   }
+  // balance sums from the deposit's exact integer totals: the momentum components and
+  // the interior mean of RHS_Part_Temp (grid.cpp:541)
+  const Geom &G = h->geom;
+  k_totals<<<1, 32, 0, h->stream>>>(f, f.totals, do_int ? 1 : 0, do_new ? 1 : 0,
+                                    1.0 / ((double)G.n[0] * G.n[1] * G.n[2]), h->mom_dev, h->emean_dev);
+  PSTEP_LAUNCHED(h);
   return PSTEP_OK;
 }
 }  // namespace

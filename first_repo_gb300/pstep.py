@@ -62,10 +62,10 @@ _D = C.POINTER(C.c_double)
 _VP = C.c_void_p
 _H = C.c_void_p
 
-EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p", "pstep_set_particle_props", "pstep_set_correction",
+EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p", "pstep_set_particle_props", "pstep_set_correction", "pstep_set_wait_limit",
            "pstep_num_particles", "pstep_bind_velocity", "pstep_bind_temperature", "pstep_prime",
            "pstep_stage_interp_advance_deposit", "pstep_wrap", "pstep_stage_temp", "pstep_stage",
-           "pstep_end_stage", "pstep_end_step", "pstep_run", "pstep_get_field", "pstep_energy_mean",
+           "pstep_end_stage", "pstep_end_step", "pstep_run", "pstep_get_field", "pstep_energy_mean", "pstep_momentum_sums",
            "pstep_get_particle_array", "pstep_last_error", "pstep_status_string", "pstep_check",
            "pstep_last_run_ms", "pstep_launch_count", "pstep_profile", "pstep_profile_read"]
 PHASES = ["advance", "deposit_int", "order", "sort", "deposit_temp", "reorder"]
@@ -83,6 +83,7 @@ def lib():
     L.pstep_set_tau_p.argtypes = [_H, _VP, C.c_int]
     L.pstep_set_particle_props.argtypes = [_H, C.POINTER(Props), C.c_int]
     L.pstep_set_correction.argtypes = [_H, C.POINTER(Correction)]
+    L.pstep_set_wait_limit.argtypes = [_H, C.c_uint32, C.c_int]
     L.pstep_num_particles.argtypes = [_H]
     L.pstep_num_particles.restype = C.c_int64
     L.pstep_bind_velocity.argtypes = [_H, _VP, _VP, _VP, C.c_int]
@@ -97,6 +98,7 @@ def lib():
     L.pstep_run.argtypes = [_H, C.c_int]
     L.pstep_get_field.argtypes = [_H, C.c_int, _VP, C.c_int]
     L.pstep_energy_mean.argtypes = [_H, _D]
+    L.pstep_momentum_sums.argtypes = [_H, _D]
     L.pstep_get_particle_array.argtypes = [_H, C.c_int, _VP, C.c_int]
     L.pstep_last_error.argtypes = [_H]
     L.pstep_last_error.restype = C.c_char_p
@@ -239,6 +241,11 @@ class ParticleStep:
         c.nu_gas = float(nu_gas if nu_gas is not None else model["nu_gas"])
         self._ok(self.L.pstep_set_correction(self.h, C.byref(c)))
 
+    def set_wait_limit(self, polls: int = 0, idle_first: bool = False):
+        """bound of the fused inference's tensor-core completion waits (0: default); idle_first
+        makes each warpgroup's first wait poll a barrier that nothing signals (timeout test)"""
+        self._ok(self.L.pstep_set_wait_limit(self.h, int(polls), 1 if idle_first else 0))
+
     @property
     def np(self) -> int:
         return int(self.L.pstep_num_particles(self.h))
@@ -280,7 +287,7 @@ class ParticleStep:
         self._ok(self.L.pstep_last_run_ms(self.h, C.byref(v)))
         return v.value
 
-    def field(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+    def field(self, name: str, out=None):
         g = self.n + 2
         if out is None:
             out = np.empty((g, g, g))
@@ -293,11 +300,21 @@ class ParticleStep:
         self._ok(self.L.pstep_energy_mean(self.h, C.byref(v)))
         return v.value
 
-    def array(self, name: str) -> np.ndarray:
+    def momentum_sums(self) -> np.ndarray:
+        """interior sums of the three deposited momentum fields of the last stage (fp64)"""
+        out = np.zeros(3)
+        self._ok(self.L.pstep_momentum_sums(self.h, out.ctypes.data_as(_D)))
+        return out
+
+    def array(self, name: str, out=None):
+        """One particle array as fp64 (int32 ids). out: a preallocated numpy array, or a
+        device buffer (a torch tensor, or an address) of np elements to fill in place."""
         n = self.np
-        out = np.empty(n, dtype=np.int32 if name == "flag" else np.float64)
+        if out is None:
+            out = np.empty(n, dtype=np.int32 if name == "flag" else np.float64)
+        p, d = _ptr(out)
         if n:
-            self._ok(self.L.pstep_get_particle_array(self.h, ARRAY_IDS[name], out.ctypes.data, 0))
+            self._ok(self.L.pstep_get_particle_array(self.h, ARRAY_IDS[name], p, d))
         return out
 
     def check(self) -> int:

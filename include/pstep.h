@@ -51,7 +51,11 @@ typedef enum {
   PSTEP_ERR_NONFINITE = 6,  /* NaN/Inf found in particle state or fields */
   PSTEP_ERR_RANGE = 7,      /* a particle position outside [0, L] (or at L, where the
                                reference indexes past its ghost layer) */
-  PSTEP_ERR_MOVE = 8,       /* a particle moved more than one cell in one stage */
+  PSTEP_ERR_MOVE = 8,       /* FP32 form: a particle's stage position more than one cell from
+                               its step-start cell along some axis (the deposit gathers each
+                               brick's sources from two cells around it, which holds only for
+                               moves of at most one cell per stage); the stage's deposits are
+                               then incomplete */
   PSTEP_ERR_NOMEM = 9,      /* device allocation failed */
   PSTEP_ERR_TIMEOUT = 10,   /* a bounded device-side wait gave up */
   PSTEP_ERR_IO = 11         /* a snapshot file could not be created, read or written */
@@ -180,6 +184,14 @@ typedef struct pstep_correction {
 } pstep_correction;
 /* NULL switches the correction off */
 int pstep_set_correction(pstep_handle h, const pstep_correction *c);
+/* The fused inference's tensor-core completion waits are bounded: after `polls` polls
+ * of an MMA's mbarrier (0: the default, 2^22) a warpgroup gives up, the kernel sets
+ * PSTEP_ERR_TIMEOUT in the check word (pstep_check), waits for the MMAs it has issued
+ * (always with the default bound), frees its tensor memory and returns. With
+ * idle_first != 0 each warpgroup's first wait polls a barrier that nothing signals, so
+ * the timeout path runs as it would for a completion that never arrives (for testing
+ * that path; the stage's results are then incomplete). No reference counterpart. */
+int pstep_set_wait_limit(pstep_handle h, uint32_t polls, int idle_first);
 int64_t pstep_num_particles(pstep_handle h);
 
 /* Gas fields, ghosted layout. The velocity is U = RU_int/Rho_face (grid.cpp:662),
@@ -222,6 +234,15 @@ int pstep_run(pstep_handle h, int nsteps);
 int pstep_get_field(pstep_handle h, int field_id, double *dst, int on_device);
 /* RHS_Part_Temp.mean() of the last stage_temp/prime (tensor0.cpp:418-435, grid.cpp:541). */
 int pstep_energy_mean(pstep_handle h, double *out);
+/* The momentum balance of the last stage's deposit: the interior sums of RHS_RU.x,
+ * .y, .z (the particles' momentum source; the gas adds it times -mp/Vcell,
+ * grid.cpp:393, and keeps the box's mean momentum with Correct_mean_RU,
+ * grid.cpp:565-577), out[0..2], in fp64. PSTEP_FP64: a fixed-order fp64 sum of the
+ * deposited values; PSTEP_FP32: the exact integer sum of the fixed-point deposits,
+ * correctly rounded (its energy mean, pstep_energy_mean, comes from the same exact
+ * totals). Zeros without TWC. Synchronises the stream. No reference counterpart as an
+ * entry point (the reference forms these means on the host inside grid). */
+int pstep_momentum_sums(pstep_handle h, double *out);
 /* Copy one particle array (PSTEP_X ... PSTEP_FLAG) to dst (int32 for PSTEP_FLAG),
  * in the reference's order when PSTEP_TRACK_ORDER is set. */
 int pstep_get_particle_array(pstep_handle h, int array_id, void *dst, int on_device);

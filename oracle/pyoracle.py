@@ -221,6 +221,81 @@ def read_records(path: str, n_cells: int) -> list[dict]:
     return recs
 
 
+def run_ref_digests(bp, case: dict, nsteps: int, dump_mode: int = 2, chunk: int = 1 << 24) -> list[dict]:
+    """Run the reference harness and digest its records as they stream out of a pipe
+    (SHA-256 of every particle array, the flags and the five ghosted fields, first 32
+    hex digits; mean(E) as a hex float), so that cases whose records are gigabytes each
+    never touch the disk. dump_mode 2: a record after every step."""
+    import hashlib
+    import threading
+    if build_ref() is None:
+        raise RuntimeError("reference sources are not available here")
+    d = tempfile.mkdtemp(prefix="pstep_refdig_")
+    pfile, ifile = write_case(d, bp, case)
+    fifo = os.path.join(d, "records.fifo")
+    os.mkfifo(fifo)
+    g3 = (bp.n + 2) ** 3
+    recs: list[dict] = []
+    err: list[BaseException] = []
+
+    def reader():
+        try:
+            with open(fifo, "rb", buffering=0) as f:
+                def take(nbytes: int) -> bytes:
+                    out = bytearray()
+                    while len(out) < nbytes:
+                        b = f.read(min(chunk, nbytes - len(out)))
+                        if not b:
+                            raise EOFError("harness output ended inside a record")
+                        out += b
+                    return bytes(out)
+
+                def digest_of(nbytes: int) -> str:
+                    h = hashlib.sha256()
+                    left = nbytes
+                    while left:
+                        b = f.read(min(chunk, left))
+                        if not b:
+                            raise EOFError("harness output ended inside an array")
+                        h.update(b)
+                        left -= len(b)
+                    return h.hexdigest()[:32]
+
+                while True:
+                    hdr = f.read(8)
+                    if not hdr:
+                        break
+                    if len(hdr) < 8:
+                        hdr += take(8 - len(hdr))
+                    tag, np_ = np.frombuffer(hdr, dtype=np.int32)
+                    rec = {"tag": int(tag), "np": int(np_), "digests": {}}
+                    for nm in ARRAYS[:32]:
+                        rec["digests"][nm] = digest_of(8 * int(np_))
+                    rec["digests"]["flag"] = digest_of(4 * int(np_))
+                    for nm in FIELDS:
+                        rec["digests"][nm] = digest_of(8 * g3)
+                    rec["mean_E"] = float(np.frombuffer(take(8), dtype=np.float64)[0])
+                    recs.append(rec)
+        except BaseException as e:  # reported after the harness ends
+            err.append(e)
+
+    t = threading.Thread(target=reader)
+    t.start()
+    try:
+        r = subprocess.run([REF_BIN, pfile, ifile, fifo, str(nsteps), str(dump_mode), "0"], capture_output=True,
+                           text=True, cwd=d)
+        t.join()
+        if r.returncode != 0:
+            raise RuntimeError("ref_harness failed:\n" + r.stdout + r.stderr)
+        if err:
+            raise err[0]
+    finally:
+        for f in os.listdir(d):
+            os.remove(os.path.join(d, f))
+        os.rmdir(d)
+    return recs
+
+
 # ---------------------------------------------------------------- snapshots and statistics
 SNAP_NAMES = ["Part_x", "Part_y", "Part_z", "Part_u", "Part_v", "Part_w", "Part_T", "Part_flag"]
 SNAP_KEYS = ["x", "y", "z", "u", "v", "w", "T", "flag"]

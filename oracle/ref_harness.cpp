@@ -29,6 +29,9 @@
 //            NP_TOT, Balance_Index, max of x y z u v w T, C and RHS_Part_Temp
 //            max/min/mean
 //
+// dump_all: 0 = records after the prime and at the end only, 1 = also after every
+// stage, 2 = also after every step (grid.cpp:315-325 done; tag 100000 + step)
+//
 // usage: ref_harness params.in input.bin output.bin nsteps dump_all [time [store_ts [load]]]
 #include <cstdio>
 #include <cstdlib>
@@ -184,7 +187,7 @@ int main(int argc, char **argv) {
       part.gas2part_Temp_new(T);
       part.Compute_RHS_Temp_new();
       part.part2gas_Temp_new(RHS_Part_Temp);
-      if (dump_all) dump(out, s * 4 + k, part, C, RHS_RU, RHS_Part_Temp, N);
+      if (dump_all == 1) dump(out, s * 4 + k, part, C, RHS_RU, RHS_Part_Temp, N);
       // grid.cpp:705-712
       part.x_int = part.x_new; part.y_int = part.y_new; part.z_int = part.z_new;
       part.u_int = part.u_new; part.v_int = part.v_new; part.w_int = part.w_new; part.T_int = part.T_new;
@@ -192,6 +195,7 @@ int main(int argc, char **argv) {
     // grid.cpp:315-325 (particle part)
     part.x = part.x_np1; part.y = part.y_np1; part.z = part.z_np1;
     part.u = part.u_np1; part.v = part.v_np1; part.w = part.w_np1; part.T = part.T_np1;
+    if (dump_all == 2) dump(out, 100000 + s, part, C, RHS_RU, RHS_Part_Temp, N);
   }
   auto t1 = std::chrono::steady_clock::now();
   if (timing) {

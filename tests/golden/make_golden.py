@@ -6,7 +6,13 @@ the single-rank MPI stub) on seeded synthetic cases and records, per call of
 the harness (prime, every stage, final state), SHA-256 digests of every array,
 plus the full final state of the smallest case.
 
-usage: python tests/golden/make_golden.py     (needs the reference sources)
+The configuration-sized case (box256_clustered: 256^3 cells, 2^24 clustered
+particles, 10 steps -- the plain FP64 drop-in's named configuration) records a
+digest of every array after the prime, after every step and at the end; its
+records (about 5 GB each) are digested as they stream out of the harness and
+written to reference_digests_box256.json.
+
+usage: python tests/golden/make_golden.py [--sized]    (needs the reference sources)
 """
 import hashlib
 import json
@@ -51,6 +57,37 @@ def make_bp(n, count, extra):
     return bp
 
 
+# name, workload (config.WORKLOADS), steps
+SIZED_CASES = [("box256_clustered", "box256_clustered", 10)]
+SIZED_FILE = os.path.join(HERE, "reference_digests_box256.json")
+
+
+def main_sized():
+    import time
+    build.build_gen()
+    if pyoracle.build_ref() is None:
+        sys.exit("reference sources not found; golden fixtures come from the reference itself")
+    out = {"generator": "first_repo_gb300/csrc/pstep_gen.c", "cases": []}
+    for name, wname, steps in SIZED_CASES:
+        wl = config.WORKLOADS[wname]
+        bp = config.box_params(wl.n, wl.n_particles, dp_over_dx=wl.dp_over_dx, mass_loading=wl.mass_loading)
+        case = gen.make_case(wl.n, wl.n_particles, wl.seed, wl.clustered, nblobs=wl.nblobs)
+        t0 = time.time()
+        recs = pyoracle.run_ref_digests(bp, case, steps, dump_mode=2)
+        entry = {
+            "name": name, "workload": wname, "n": wl.n, "count": wl.n_particles, "seed": wl.seed,
+            "clustered": wl.clustered, "nblobs": wl.nblobs, "steps": steps, "step_config": bp.step_config(),
+            "inputs": {k: digest(case[k]) for k in ("ux", "uy", "uz", "T", "x", "y", "z", "u", "v", "w", "t", "flag")},
+            "reference_seconds": round(time.time() - t0, 1),
+            "records": [{"tag": r["tag"], "np": r["np"], "mean_E": r["mean_E"].hex(),
+                         "digests": {k: r["digests"][k] for k in STATE}} for r in recs],
+        }
+        out["cases"].append(entry)
+        print(name, "records", len(recs), f"{time.time() - t0:.0f} s")
+    with open(SIZED_FILE, "w") as f:
+        json.dump(out, f, indent=1)
+
+
 def main():
     build.build_gen()
     if pyoracle.build_ref() is None:
@@ -81,4 +118,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--sized" in sys.argv:
+        main_sized()
+    else:
+        main()

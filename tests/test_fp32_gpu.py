@@ -64,6 +64,15 @@ def compare(o, g, L):
         out[f] = helpers.max_rel_to_max(a, b)
     me, mo = g.energy_mean(), o.mean(o.fields["E"])
     out["mean_E"] = abs(me - mo) / max(abs(mo), 1e-300)
+    # the momentum balance against the oracle's deposits, relative to the sum of magnitudes,
+    # and against the form's own deposited fields (the exact integer totals, rounded once)
+    mom = g.momentum_sums()
+    for d, f in enumerate(("Ax", "Ay", "Az")):
+        ref = o.fields[f][1:-1, 1:-1, 1:-1]
+        own = g.field(helpers.FIELD_MAP[f])[1:-1, 1:-1, 1:-1]
+        scale = max(float(np.sum(np.abs(ref))), 1e-300)
+        out["mom_" + f] = abs(mom[d] - float(np.sum(ref))) / scale
+        assert abs(mom[d] - float(np.sum(own))) <= 1e-12 * scale
     return out
 
 

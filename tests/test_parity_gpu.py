@@ -53,6 +53,18 @@ def compare_exact(o, g, where, exact_fields=True):
             assert helpers.max_rel_to_max(a, b) <= DEPOSIT_TOL, f"{where}: field {f} {helpers.max_rel_to_max(a, b):.3e}"
     me, mo = g.energy_mean(), o.mean(o.fields["E"])
     assert abs(me - mo) <= MEAN_RTOL * max(abs(mo), 1e-300), f"{where}: energy mean {me} vs {mo}"
+    check_momentum_sums(o, g, where)
+
+
+def check_momentum_sums(o, g, where, rtol=MEAN_RTOL):
+    """The per-stage momentum balance (pstep_momentum_sums): interior sums of the three
+    deposited momentum fields, within rtol of the sum of their magnitudes (the sums
+    cancel, so a relative bound on the sum itself would be meaningless)."""
+    got = g.momentum_sums()
+    for d, f in enumerate(("Ax", "Ay", "Az")):
+        interior = o.fields[f][1:-1, 1:-1, 1:-1]
+        want, scale = float(np.sum(interior)), float(np.sum(np.abs(interior)))
+        assert abs(got[d] - want) <= rtol * max(scale, 1e-300), f"{where}: momentum sum {f} {got[d]} vs {want}"
 
 
 @pytest.mark.parametrize("name", ["box12_small", "box16_twc_off_gravity", "box32_clustered", "box64_uniform"])
