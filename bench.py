@@ -57,9 +57,13 @@ FP64_ADVANCE_CELL_BYTES = 4 * 8
 FP32_ADVANCE_BYTES = {0: 36 + 80, 1: 100 + 80, 2: 100 + 80, 3: 100 + 80}
 FP32_ADVANCE_CELL_BYTES = 4 * 4
 # with the learned correction the advance also reads and writes the drive state
-# (slip 3 + temperature difference, fp32) of every particle: +32 B per particle and stage;
-# the network's weights (13 KB) are read once per CTA.
-FP32MLP_ADVANCE_EXTRA = 32
+# (slip 3 + temperature difference, fp32) and reads the kept network output (bf16 x 4):
+# +40 B per particle and stage.
+FP32MLP_ADVANCE_EXTRA = 40
+# The network kernel (once per step): x_int cell + offsets + u,v,w (28 B), the drive state
+# (16 B), the network output written (8 B) = 52 B per particle; the velocity field (3 fp32)
+# once per launch; the weights (13 KB) once per CTA.
+FP32MLP_NETWORK_BYTES = (52.0, 12.0)
 # Deposits, per particle and per cell of one launch:
 #   FP32 (one fused walk): *_int cell+offsets (16) + RHS_u (12) + *_new cell+offsets (16) + RHS_T (4) = 48 B;
 #        per cell: cell_start (4) + five fp64 fields written (40) = 44 B.
@@ -72,6 +76,7 @@ PHASE_BYTES = {
     ("fp32", "deposit_int"): (48.0, 44.0),
     ("fp32mlp", "advance"): (sum(FP32_ADVANCE_BYTES.values()) / 4.0 + FP32MLP_ADVANCE_EXTRA, FP32_ADVANCE_CELL_BYTES),
     ("fp32mlp", "deposit_int"): (48.0, 44.0),
+    ("fp32mlp", "network"): FP32MLP_NETWORK_BYTES,
     ("fp64", "advance"): (sum(FP64_ADVANCE_BYTES.values()) / 4.0, FP64_ADVANCE_CELL_BYTES),
     ("fp64", "deposit_int"): (52.0, 36.0),
     ("fp64", "deposit_temp"): (36.0, 12.0),

@@ -79,6 +79,7 @@ struct pstep_ctx {
   int64_t cap;
   int num_sms;
   int corr_on;                              // learned correction active (FP32 form)
+  int corr_every_stage;                     // run the network at every stage (else stage 0 only)
   uint32_t wait_limit;                      // polls of the tensor-core completion waits (0: default)
   int wait_idle;                            // timeout test: first wait polls a barrier nothing signals
   alignas(16) unsigned char corr_dev[256];  // its kernel constants (stage_f32.cu)

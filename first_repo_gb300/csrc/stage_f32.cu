@@ -55,11 +55,14 @@ struct Set32 {
   float *v[4];  // u v w T
 };
 
-// Deposit bricks (the cells one CTA owns) are BR^3 with BR = 16 where the grid
-// allows (every side a multiple of 16, at least 32 cells: the source window of
-// BR + 4 cells must not wrap onto itself), else 8. A brick's source particles
-// (those whose step-start cell lies within two cells of it) are visited about
-// ((BR+4)/BR)^3 times each: 1.95 at BR = 16, 3.4 at BR = 8.
+// Deposit bricks (the cells one CTA owns) are BR x BR x BZ: 16 x 16 x 8 where the
+// grid allows (x and y sides multiples of 16 and at least 32 cells, z a multiple of 8
+// and at least 16: a source window of the brick and two cells around it must not
+// wrap onto itself), else 8 x 8 x 8. A brick's source particles (those whose
+// step-start cell lies within two cells of it) are visited about
+// (BR+4)^2 (BZ+4) / (BR^2 BZ) times each: 2.34 for 16 x 16 x 8, 3.4 for 8^3. The
+// 16 x 16 x 8 shape keeps the five fields' accumulators (brick plus one cell) in the
+// shared memory of one CTA, so one walk deposits all of them.
 //
 // Work list of the deposit: one item per deposit brick, or -- for bricks whose
 // source window holds more than kChunkMax particles -- several items, each a
@@ -67,12 +70,12 @@ struct Set32 {
 // come first (largest work first), then the rest; CTAs take items in order from
 // an atomic counter. kVisit bounds the visits per particle (windows overlap), so
 // at most kVisit * particles / kChunkMax bricks split.
-template <int BR> struct DepTraits;
-template <> struct DepTraits<8> {
+template <int BR, int BZ> struct DepTraits;
+template <> struct DepTraits<8, 8> {
   static constexpr int kThreads = 256, kVisit = 4;  // (12/8)^3 = 3.4
 };
-template <> struct DepTraits<16> {
-  static constexpr int kThreads = 1024, kVisit = 2;  // (20/16)^3 = 1.95
+template <> struct DepTraits<16, 8> {
+  static constexpr int kThreads = 1024, kVisit = 3;  // (20/16)^2 (12/8) = 2.34
 };
 
 struct Work {
@@ -83,9 +86,9 @@ struct Work {
   int32_t *n_items;     // device scalar
   int32_t *next;        // device counters, one per deposit launch
   int32_t *done;        // per slot: items finished
-  long long *tiles;     // per slot: 5 x BR^3 int64
+  long long *tiles;     // per slot: 5 x BR^2 BZ int64
   int64_t slot_cap;
-  int br;               // deposit brick edge, 8 or 16
+  int br, bz;           // deposit brick edges: 16 x 16 x 8 or 8 x 8 x 8
   int nbd;              // number of deposit bricks
   int32_t *err;         // device error word (kErrCapacity)
 };
@@ -372,20 +375,22 @@ __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int
 }
 
 // ----------------------------------------------------------------------------
-// The learned correction fused into the advance (pstep_set_correction).
+// The learned correction (pstep_set_correction).
 //
-// Stage 0 runs the network: persistent CTAs of two warpgroups; each warpgroup
-// owns tiles of 128 particles, one particle per thread, and thread t's network
-// row is tensor-memory lane t of the warpgroup's 64 columns. Per tile: the plain
-// interpolation and the features in registers, the feature row as bf16 to shared
-// memory, three tcgen05 MMAs (16 -> 64 -> 64 -> 16 columns; each layer's
-// accumulator reuses the columns of the one before, which has been read), bias
-// and SiLU between them on 16-column chunks, then the corrected gas values feed
-// the same finish as the plain step. The two warpgroups synchronise with named
-// barriers only, so one's MMAs overlap the other's loads and epilogues. The
-// network output (bf16 x 4) is kept per particle for stages 1-3, which apply it
-// with their own drive slip and prior: within a step a particle moves less than
-// a few hundredths of a cell and its slip hardly changes.
+// The network runs in its own kernel, k_corr_net, at stage 0 of every step (or at
+// every stage, pstep_correction.every_stage): persistent CTAs of two warpgroups;
+// each warpgroup owns tiles of 128 particles, one particle per thread, and thread
+// t's network row is tensor-memory lane t of the warpgroup's 64 columns. Per tile:
+// the plain interpolation at x_int and the features in registers, the feature row
+// as bf16 to shared memory, three tcgen05 MMAs (16 -> 64 -> 64 -> 16 columns; each
+// layer's accumulator reuses the columns of the one before, which has been read),
+// bias and SiLU between them on 16-column chunks, and the network output (bf16 x 4,
+// zero for particles outside the training ranges) to memory. The two warpgroups
+// synchronise with named barriers only, so one's MMAs overlap the other's loads and
+// epilogues; four CTAs per SM keep eight warpgroups in flight. The advance of every
+// stage (k_advance32_corr) applies the kept output with that stage's own drive slip
+// and prior: within a step a particle moves a few hundredths of a cell and its slip
+// hardly changes, so one inference per step serves the step's four stages.
 // Particles outside the training ranges keep the plain interpolation.
 namespace corr {
 constexpr int kRows = 128, kInP = 16, kHid = 64, kOutP = 16, kGroups = 2, kThreads = kRows * kGroups;
@@ -516,9 +521,12 @@ __device__ __forceinline__ float particle_dp(const F32Form &f, const CorrDev &cd
   return f.pp[PP_ITTH] ? itth * cd.dp_per_itth : cd.dp;
 }
 
+// The network of every particle at its x_int position: features from the plain
+// interpolation and the drive state of the previous stage, three tcgen05 layers,
+// the output (bf16 x 4) to f.corr_y (zero outside the training ranges).
 template <int K>
-__global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32Form f, C32 c, int twc, int64_t n,
-                                                                     int32_t *__restrict__ err, CorrDev cd) {
+__global__ void __launch_bounds__(corr::kThreads, 4) k_corr_net(Geom G, F32Form f, C32 c, int64_t n,
+                                                                int32_t *__restrict__ err, CorrDev cd) {
   extern __shared__ __align__(1024) uint8_t sm[];
   using namespace tc05;
   const int tid = threadIdx.x, wg = tid >> 7, lt = tid & (corr::kRows - 1), warp = tid >> 5;
@@ -550,25 +558,22 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
   uint32_t phase = 0;
   bool ok = true;
   bool first = cd.idle_first != 0;
-  float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
   const int64_t ntiles = (n + corr::kRows - 1) / corr::kRows;
   for (int64_t tile = (int64_t)blockIdx.x * corr::kGroups + wg; tile < ntiles && ok;
        tile += (int64_t)gridDim.x * corr::kGroups) {
     const int64_t p = tile * corr::kRows + lt;
     const bool live = p < n;
-    // phase A: the plain interpolation and the features; only these stay live across the MMAs
-    Adv a;
-    float sdrv = 0.f, prior = 1.f, smag = 0.f;
     bool use = false;
     {
       float x[corr::kInP];
 #pragma unroll
       for (int j = 0; j < corr::kInP; ++j) x[j] = 0.f;
       if (live) {
+        Adv a;
         adv_load_gas<K>(G, f, p, a);
         const float s[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
-        smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
-        float dir[3], dmag;
+        const float smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+        float sdrv, dir[3], dmag;
         drive_slip(f, p, s, smag, sdrv, dir, dmag);
         const float itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
         const float itp = f.itp ? f.itp[p] : c.itp;
@@ -578,7 +583,6 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
         const float rep = sdrv * particle_dp(f, cd, p, itth) * cd.inv_nu;
         const float q = alpha * his;
         const float taup = 1.f / itp;
-        prior = prior_of(cd, dpdx, rep);
         use = smag > 0.f && dmag > 0.f && dpdx >= cd.lo[0] && dpdx <= cd.hi[0] && rep >= cd.lo[1] &&
               rep <= cd.hi[1] && q >= cd.lo[2] && q <= cd.hi[2] && taup >= cd.lo[3] && taup <= cd.hi[3];
         if (use) {
@@ -643,37 +647,26 @@ __global__ void __launch_bounds__(corr::kThreads, 3) k_advance32_mlp(Geom G, F32
     tmem_ld16(tl, y);
     tc05::fence_before();  // the accumulator reads before the warpgroup's next MMA
     if (live) {
-      // phase B: the rest of the particle, the correction, the finish
-      adv_load_rest<K>(G, f, c, p, a);
       float yo[4] = {0.f, 0.f, 0.f, 0.f};
-      float ty = 0.f;
       if (use) {
 #pragma unroll
         for (int d = 0; d < 4; ++d) yo[d] = y[d] + b3[d];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) a.gas[d] -= sdrv * prior * yo[d];
-        ty = prior * yo[3];
       }
       f.corr_y[p] = make_uint2(pack_bf16x2(yo[0], yo[1]), pack_bf16x2(yo[2], yo[3]));
-      f.drive[0][p] = a.vin[0] - a.gas[0];
-      f.drive[1][p] = a.vin[1] - a.gas[1];
-      f.drive[2][p] = a.vin[2] - a.gas[2];
-      f.drive[3][p] = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, use ? f.drive[3][p] : 0.f, err, mu0, mu1, mu2, mt);
     }
   }
   if (!ok) {
     if (lt == 0) atomicOr(err, kErrTimeout);
-    tc05::mbar_wait(mbar, phase, corr::kWaitLimit);
+    tc05::mbar_wait(mbar, phase, corr::kWaitLimit);  // the MMA issued before the wait ran out
   }
-  block_max4(f.slots, mu0, mu1, mu2, mt);
   tc05::fence_before();
   __syncthreads();
   tc05::fence_after();
   if (warp == 0) tmem_dealloc(*tslot, 128);
 }
 
-// stages 1-3 with the correction: the network output of the step's stage 0, applied with
-// this stage's drive slip and prior
+// every stage with the correction: the kept network output, applied with this stage's
+// drive slip and prior
 template <int K>
 __global__ void __launch_bounds__(256, 5) k_advance32_corr(Geom G, F32Form f, C32 c, int twc, int64_t n,
                                                         int32_t *__restrict__ err, CorrDev cd) {
@@ -819,15 +812,15 @@ __device__ __forceinline__ long long get_fixed(const uint32_t *lo, const uint32_
   return (long long)(int32_t)*hi * 65536ll + (long long)*lo;
 }
 
-// Accumulator of a deposit brick: its BR^3 cells and one cell around them,
-// brick-relative x, y, z in [-1, BR], rows padded by one word so that neighbouring
-// rows do not fall on the same shared-memory banks. A particle whose every target
-// lies in this region adds without a per-target test; what lands in the outer
-// layer is not read (the neighbouring brick counts it for its own cells).
-template <int BR> struct Acc {
-  static constexpr int kSide = BR + 2, kRow = BR + 3, kSlots = kRow * kSide * kSide;
+// Accumulator of a deposit brick: its BR x BR x BZ cells and one cell around them,
+// brick-relative x, y in [-1, BR], z in [-1, BZ], rows padded by one word so that
+// neighbouring rows do not fall on the same shared-memory banks. A particle whose
+// every target lies in this region adds without a per-target test; what lands in
+// the outer layer is not read (the neighbouring brick counts it for its own cells).
+template <int BR, int BZ> struct Acc {
+  static constexpr int kSideY = BR + 2, kSideZ = BZ + 2, kRow = BR + 3, kSlots = kRow * kSideY * kSideZ;
   static __device__ __forceinline__ int slot(int x, int y, int z) {
-    return ((z + 1) * kSide + (y + 1)) * kRow + (x + 1);
+    return ((z + 1) * kSideY + (y + 1)) * kRow + (x + 1);
   }
 };
 
@@ -836,12 +829,13 @@ template <int BR> struct Acc {
 // BR/8 runs of 8 cells, then [b+BR, b+BR+1]. Each segment lies in one 8^3 sort
 // brick along one x-row, so its particles are one contiguous range
 // [cell_start[id], cell_start[id + len]) of the sorted order.
-template <int BR> struct Window {
-  static constexpr int kSeg = 2 + BR / kBr, kSide = BR + 2 * kHalo, kRanges = kSide * kSide * kSeg;
+template <int BR, int BZ> struct Window {
+  static constexpr int kSeg = 2 + BR / kBr, kSideY = BR + 2 * kHalo, kSideZ = BZ + 2 * kHalo,
+                       kRanges = kSideY * kSideZ * kSeg;
   static __device__ __forceinline__ void segment(const Geom &G, int bx, int by, int bz, int r, uint32_t &id,
                                                  int &len) {
     const int sg = r % kSeg, row = r / kSeg;
-    int j = by - kHalo + row % kSide, k = bz - kHalo + row / kSide;
+    int j = by - kHalo + row % kSideY, k = bz - kHalo + row / kSideY;
     j += j < 0 ? G.n[1] : 0; j -= j >= G.n[1] ? G.n[1] : 0;
     k += k < 0 ? G.n[2] : 0; k -= k >= G.n[2] ? G.n[2] : 0;
     int x0;
@@ -853,20 +847,29 @@ template <int BR> struct Window {
   }
 };
 
+// deposit brick b's origin (cells)
+template <int BR, int BZ>
+__device__ __forceinline__ void brick_origin(const Geom &G, int b, int &bx, int &by, int &bz) {
+  const int ndx = G.n[0] / BR, ndy = G.n[1] / BR;
+  bx = (b % ndx) * BR;
+  by = ((b / ndx) % ndy) * BR;
+  bz = (b / (ndx * ndy)) * BZ;
+}
+
 // per deposit brick: the particles of its source window (one warp per brick) and
 // from that the number of work items, each at most kChunkMax particles
-template <int BR>
+template <int BR, int BZ>
 __global__ void k_work_count(Geom G, const int32_t *__restrict__ cs, Work w, int nb) {
   const int lane = threadIdx.x & 31;
   const int b = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (b >= nb) return;  // whole warps
-  const int ndx = G.n[0] / BR, ndy = G.n[1] / BR;
-  const int bx = (b % ndx) * BR, by = ((b / ndx) % ndy) * BR, bz = (b / (ndx * ndy)) * BR;
+  int bx, by, bz;
+  brick_origin<BR, BZ>(G, b, bx, by, bz);
   long long total = 0;
-  for (int r = lane; r < Window<BR>::kRanges; r += 32) {
+  for (int r = lane; r < Window<BR, BZ>::kRanges; r += 32) {
     uint32_t id;
     int len;
-    Window<BR>::segment(G, bx, by, bz, r, id, len);
+    Window<BR, BZ>::segment(G, bx, by, bz, r, id, len);
     total += cs[id + len] - cs[id];
   }
 #pragma unroll
@@ -901,12 +904,13 @@ __global__ void k_work_fill(Work w, int nb) {
 }
 
 // trilinear deposit (particle.cpp:526-559, :586-658) of a particle with in-cell offsets
-// o3 whose round() node is `node` (brick-relative, each axis in [0, BR]) and value `val`
-// (already times the field's fixed-point scale): the 8 cells node - 1 .. node get
-// products of x_l / (1 - x_l), all inside the accumulator region
-template <int BR>
+// o3 whose round() node is `node` (brick-relative, in [0, BR] x [0, BR] x [0, BZ]) and
+// value `val` (already times the field's fixed-point scale): the 8 cells node - 1 ..
+// node get products of x_l / (1 - x_l), all inside the accumulator region
+template <int BR, int BZ>
 __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, const int node[3], const float o3[3],
                                                   float val) {
+  using A = Acc<BR, BZ>;
   float w[3][2];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -914,7 +918,7 @@ __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, co
     w[d][0] = 1.f - xl;  // cell node - 1
     w[d][1] = xl;        // cell node
   }
-  const int base = Acc<BR>::slot(node[0] - 1, node[1] - 1, node[2] - 1);
+  const int base = A::slot(node[0] - 1, node[1] - 1, node[2] - 1);
 #pragma unroll
   for (int oz = 0; oz < 2; ++oz)
 #pragma unroll
@@ -922,20 +926,21 @@ __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, co
       const float wyz = w[2][oz] * w[1][oy] * val;
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) {
-        const int sl = base + (oz * Acc<BR>::kSide + oy) * Acc<BR>::kRow + ox;
+        const int sl = base + (oz * A::kSideY + oy) * A::kRow + ox;
         add_fixed32(lo + sl, hi + sl, __float2int_rn(w[0][ox] * wyz));
       }
     }
 }
 
 // face-normal deposits (particle.cpp:498-524) of a particle in brick-relative cell r3
-// (each axis in [-1, BR - 1]): along d, face r3[d] gets (1 - x_l) R_d and face
-// r3[d] + 1 gets x_l R_d, at the particle's cell across. lo[d]/hi[d]: field d's words.
-template <int BR>
+// (in [-1, BR - 1] x [-1, BR - 1] x [-1, BZ - 1]): along d, face r3[d] gets (1 - x_l) R_d
+// and face r3[d] + 1 gets x_l R_d, at the particle's cell across. lo[d]/hi[d]: field d's words.
+template <int BR, int BZ>
 __device__ __forceinline__ void deposit_faces(uint32_t *const *lo, uint32_t *const *hi, const int r3[3],
                                               const float o3[3], const float ru[3], const float *scale) {
-  const int sl0 = Acc<BR>::slot(r3[0], r3[1], r3[2]);
-  constexpr int step[3] = {1, Acc<BR>::kRow, Acc<BR>::kSide * Acc<BR>::kRow};
+  using A = Acc<BR, BZ>;
+  const int sl0 = A::slot(r3[0], r3[1], r3[2]);
+  constexpr int step[3] = {1, A::kRow, A::kSideY * A::kRow};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float r = ru[d] * scale[1 + d];
@@ -975,15 +980,15 @@ __device__ __forceinline__ void block_exclusive_scan2(int32_t *a, int n, int32_t
   __syncthreads();
 }
 
-// Shared memory of the deposit CTA for brick edge BR: the accumulator of the widest
-// pass (NF fields, two words per slot; a multiple of 8 bytes), block-reduction
-// scratch (32 int64), the window's row-segment prefix and starts, misc words.
-template <int BR, int NF> struct DepSmem {
-  static constexpr int kRanges = Window<BR>::kRanges;
-  static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR>::kSlots;
+// Shared memory of the deposit CTA for bricks BR x BR x BZ: the accumulators of the NF
+// fields (two words per slot; a multiple of 8 bytes), block-reduction scratch (32
+// int64), the window's row-segment prefix and starts, misc words.
+template <int BR, int BZ, int NF> struct DepSmem {
+  static constexpr int kRanges = Window<BR, BZ>::kRanges;
+  static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR, BZ>::kSlots;
   static constexpr size_t kBytes =
       2 * kAcc + sizeof(long long) * 32 + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
-  static_assert(kRanges <= 2 * DepTraits<BR>::kThreads, "ranges exceed the block scan");
+  static_assert(kRanges <= 2 * DepTraits<BR, BZ>::kThreads, "ranges exceed the block scan");
 };
 
 // block sum of one int64 per thread; every thread calls it, thread 0 gets the result
@@ -996,33 +1001,32 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *scrat
   __syncthreads();
   long long s = 0;
   if (threadIdx.x == 0)
-    for (int q = 0; q < nw; ++q) s += scratch[q];  // fixed order (integer: exact anyway)
+    for (int q = 0; q < nw; ++q) s += scratch[q];  // integer sums: exact in any order
   return s;
 }
 
-// Deposit into bricks of BR^3 interior cells. A work item walks its brick's source
-// window (the particles whose step-start cell lies within two cells of the brick)
-// once per pass:
-//   pass A (DO_INT): the concentration and the face momentum at the *_int positions
-//     (fields C, RHS_RU x/y/z); a particle counts when its x_int cell lies within one
-//     cell of the brick -- its trilinear node in [0, BR] and, for the faces, its cell
-//     in [-1, BR - 1] -- and then adds every target without a test;
-//   pass B (DO_NEW): RHS_T at the *_new positions (RHS_Part_Temp), the same way.
-// Scale exponents f.se[0..4]. Each brick's exact integer field totals are added to
-// `totals` (five int64 words, zeroed before the launch): the momentum and energy
-// balance sums, exact and independent of the order of the work.
-template <bool DO_INT, bool DO_NEW, int BR>
-__global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w,
-                                                                   int twc, double *__restrict__ outC,
-                                                                   double *__restrict__ outX,
-                                                                   double *__restrict__ outY,
-                                                                   double *__restrict__ outZ,
-                                                                   double *__restrict__ outE,
-                                                                   unsigned long long *__restrict__ totals) {
-  constexpr int NF = DO_INT ? 4 : 1;  // fields of the widest pass
-  constexpr int NB3 = BR * BR * BR;
-  constexpr int SLOTS = Acc<BR>::kSlots;
-  constexpr int NR = Window<BR>::kRanges;
+// Deposit into bricks of BR x BR x BZ interior cells, one walk over each brick's
+// source window (the particles whose step-start cell lies within two cells of the
+// brick). Per particle, every value the walk may need is loaded at once; then
+//   DO_INT: the concentration and the face momentum at the *_int position (fields
+//     C, RHS_RU x/y/z) count when its x_int cell lies within one cell of the brick --
+//     the trilinear node in the brick's node range, the cell in [-1, B - 1] for the
+//     faces -- and add every target without a test;
+//   DO_NEW: RHS_T at the *_new position (RHS_Part_Temp), the same way.
+// Field slots: 0 C, 1-3 RHS_RU x/y/z, 4 (FE) RHS_Part_Temp; scale exponents f.se[0..4].
+// Each brick's exact integer field totals are added to `totals` (five int64 words,
+// zeroed before the launch): the momentum and energy balance sums, exact and
+// independent of the order of the work.
+template <bool DO_INT, bool DO_NEW, int BR, int BZ>
+__global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
+    k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w, int twc, double *__restrict__ outC,
+            double *__restrict__ outX, double *__restrict__ outY, double *__restrict__ outZ,
+            double *__restrict__ outE, unsigned long long *__restrict__ totals) {
+  constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
+  constexpr int FE = DO_INT ? 4 : 0;  // accumulator index of RHS_Part_Temp
+  constexpr int NB = BR * BR * BZ;
+  constexpr int SLOTS = Acc<BR, BZ>::kSlots;
+  constexpr int NR = Window<BR, BZ>::kRanges;
   extern __shared__ __align__(16) uint8_t dsm[];
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(dsm);
   uint32_t *acc_hi = acc_lo + NF * SLOTS;
@@ -1030,18 +1034,20 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
   int32_t *pre = reinterpret_cast<int32_t *>(red + 32);                 // NR + 1
   int32_t *beg = pre + NR + 1;                                          // NR
   int32_t *misc = beg + NR;                                             // 32 warp sums, item, last
-  uint32_t *lo_f[4], *hi_f[4];
+  uint32_t *lo_f[5], *hi_f[5];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 5; ++q) {
     lo_f[q] = acc_lo + (q < NF ? q : 0) * SLOTS;
     hi_f[q] = acc_hi + (q < NF ? q : 0) * SLOTS;
   }
-  double *const outs[5] = {outC, outX, outY, outZ, outE};
-  const int ndx = G.n[0] / BR, ndy = G.n[1] / BR;
   const int32_t n_items = *w.n_items;
   float scale[5];
 #pragma unroll
   for (int q = 0; q < 5; ++q) scale[q] = ldexpf(1.0f, f.se[q]);  // exact powers of two
+  int se[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) se[q] = f.se[q];
+  const bool ru_on = DO_INT && twc;
   while (true) {
     if (threadIdx.x == 0) misc[32] = atomicAdd(&w.next[0], 1);
     __syncthreads();
@@ -1051,14 +1057,18 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     if (item < 0) { __syncthreads(); continue; }
     const int brick = (int)(item >> 32), chunk = (int)(item & 0xffffffffll);
     const int nch = w.nchunk[brick];
-    const int bx = (brick % ndx) * BR, by = ((brick / ndx) % ndy) * BR, bz = (brick / (ndx * ndy)) * BR;
-    const int b3[3] = {bx, by, bz};
+    int bx, by, bz;
+    brick_origin<BR, BZ>(G, brick, bx, by, bz);
     const int slot_idx = nch > 1 ? w.slot[brick] : -1;
-    long long *tile = slot_idx >= 0 ? w.tiles + (int64_t)slot_idx * 5 * NB3 : nullptr;
+    long long *tile = slot_idx >= 0 ? w.tiles + (int64_t)slot_idx * 5 * NB : nullptr;
+    for (int s = threadIdx.x; s < NF * SLOTS; s += blockDim.x) {
+      acc_lo[s] = 0u;
+      acc_hi[s] = 0u;
+    }
     for (int r = threadIdx.x; r < NR; r += blockDim.x) {
       uint32_t id;
       int len;
-      Window<BR>::segment(G, bx, by, bz, r, id, len);
+      Window<BR, BZ>::segment(G, bx, by, bz, r, id, len);
       const int32_t a0 = f.cell_start[id];
       beg[r] = a0;
       pre[r] = f.cell_start[id + len] - a0;
@@ -1079,127 +1089,109 @@ __global__ void __launch_bounds__(DepTraits<BR>::kThreads) k_dep32(Geom G, F32Fo
     const int32_t g1 = t0 + (int32_t)(((int64_t)(t1 - t0) * (grp + 1)) / ngroups);
     // segment of the thread's first particle: the last r with pre[r] <= t (binary
     // search); later particles only move forward (pre[NR] = total > t ends the scan)
-    int seg0 = 0;
+    int seg = 0;
     {
       const int32_t tf = g0 + (int32_t)(threadIdx.x & 7);
       int hi = NR;
-      while (hi - seg0 > 1) {
-        const int mid = (seg0 + hi) >> 1;
-        if (pre[mid] <= tf) seg0 = mid; else hi = mid;
+      while (hi - seg > 1) {
+        const int mid = (seg + hi) >> 1;
+        if (pre[mid] <= tf) seg = mid; else hi = mid;
       }
     }
-#pragma unroll 1
-    for (int pass = DO_INT ? 0 : 1; pass <= (DO_NEW ? 1 : 0); ++pass) {
-      const int nf = pass == 0 ? 4 : 1;  // accumulated fields of this pass
-      for (int s = threadIdx.x; s < nf * SLOTS; s += blockDim.x) {
-        acc_lo[s] = 0u;
-        acc_hi[s] = 0u;
-      }
-      __syncthreads();
-      int seg = seg0;
-      const uint32_t *__restrict__ cellp = pass == 0 ? SI.cell : SN.cell;
-      const float *__restrict__ op0 = pass == 0 ? SI.o[0] : SN.o[0];
-      const float *__restrict__ op1 = pass == 0 ? SI.o[1] : SN.o[1];
-      const float *__restrict__ op2 = pass == 0 ? SI.o[2] : SN.o[2];
-      for (int32_t t = g0 + (int32_t)(threadIdx.x & 7); t < g1; t += 8) {
-        while (pre[seg + 1] <= t) ++seg;
-        const int32_t p = beg[seg] + (t - pre[seg]);
-        const uint32_t c = cellp[p];
-        int r3[3];
-        r3[0] = rel_local(ci_(c), b3[0], G.n[0]);
-        r3[1] = rel_local(cj_(c), b3[1], G.n[1]);
-        r3[2] = rel_local(ck_(c), b3[2], G.n[2]);
-        // only a cell within one of the brick ([-1, BR] per axis) reaches it; then every
-        // target of the particle lies in the accumulator
-        if ((unsigned)(r3[0] + 1) > (unsigned)(BR + 1) || (unsigned)(r3[1] + 1) > (unsigned)(BR + 1) ||
-            (unsigned)(r3[2] + 1) > (unsigned)(BR + 1))
-          continue;
-        const float o3[3] = {op0[p], op1[p], op2[p]};
-        const int node[3] = {r3[0] + (o3[0] >= 0.5f ? 1 : 0), r3[1] + (o3[1] >= 0.5f ? 1 : 0),
-                             r3[2] + (o3[2] >= 0.5f ? 1 : 0)};
-        // trilinear targets node - 1 .. node meet the brick iff the node is in [0, BR]
-        const bool tri = (unsigned)node[0] <= (unsigned)BR && (unsigned)node[1] <= (unsigned)BR &&
-                         (unsigned)node[2] <= (unsigned)BR;
-        if (pass == 0) {
-          if (tri) deposit_trilinear<BR>(lo_f[0], hi_f[0], node, o3, scale[0]);
-          // faces r3 .. r3 + 1 along d, r3 across, meet the brick iff r3 is in [-1, BR - 1]
-          if (twc && r3[0] < BR && r3[1] < BR && r3[2] < BR) {
-            const float ru[3] = {f.rhs_u[0][p], f.rhs_u[1][p], f.rhs_u[2][p]};
-            deposit_faces<BR>(&lo_f[1], &hi_f[1], r3, o3, ru, scale);
-          }
-        } else if (tri) {
-          deposit_trilinear<BR>(lo_f[0], hi_f[0], node, o3, f.rhs_t[p] * scale[4]);
-        }
-      }
-      __syncthreads();
-      // this pass's fields: into the split brick's global tile, or written out
-      const int fbase = pass == 0 ? 0 : 4;
-      if (tile) {
-        for (int s = threadIdx.x; s < nf * NB3; s += blockDim.x) {
-          const int q = s / NB3, r = s % NB3;
-          const int sl = q * SLOTS + Acc<BR>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
-          const long long v = get_fixed(&acc_lo[sl], &acc_hi[sl]);
-          if (v) atomicAdd((unsigned long long *)&tile[(fbase + q) * NB3 + r], (unsigned long long)v);
-        }
-      } else {
-        long long tot[4] = {0, 0, 0, 0};
-        double *const dst[4] = {pass == 0 ? outC : outE, outX, outY, outZ};
-        int se[4];
+    for (int32_t t = g0 + (int32_t)(threadIdx.x & 7); t < g1; t += 8) {
+      while (pre[seg + 1] <= t) ++seg;
+      const int32_t p = beg[seg] + (t - pre[seg]);
+      // all loads first: one memory round trip per particle
+      uint32_t ci = 0, cn = 0;
+      float oi[3] = {0.f, 0.f, 0.f}, on3[3] = {0.f, 0.f, 0.f}, ru[3] = {0.f, 0.f, 0.f}, rt = 0.f;
+      if (DO_INT) {
+        ci = SI.cell[p];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) se[q] = f.se[pass == 0 ? q : 4];
-        const bool zero_ru = pass == 0 && !twc;  // RHS_RU = 0 without TWC (grid.cpp:671)
-        for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
-          const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
-          const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
-          const int sl = Acc<BR>::slot(lx, ly, lz);
+        for (int d = 0; d < 3; ++d) oi[d] = SI.o[d][p];
+        if (ru_on) {
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (q >= nf) break;
-            const long long v = get_fixed(&lo_f[q][sl], &hi_f[q][sl]);
-            const bool z = q >= 1 && zero_ru;
-            dst[q][g] = z ? 0.0 : fixed_to_f64(v, se[q]);
-            tot[q] += z ? 0 : v;
-          }
-        }
-        for (int q = 0; q < nf; ++q) {
-          const long long s = block_sum_i64(tot[q], red);
-          if (threadIdx.x == 0 && s) atomicAdd(&totals[fbase + q], (unsigned long long)s);
+          for (int d = 0; d < 3; ++d) ru[d] = f.rhs_u[d][p];
         }
       }
-      __syncthreads();  // the accumulator is read before the next pass clears it
+      if (DO_NEW) {
+        cn = SN.cell[p];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) on3[d] = SN.o[d][p];
+        rt = f.rhs_t[p];
+      }
+      if (DO_INT) {
+        const int r3[3] = {rel_local(ci_(ci), bx, G.n[0]), rel_local(cj_(ci), by, G.n[1]),
+                           rel_local(ck_(ci), bz, G.n[2])};
+        // only a cell within one of the brick reaches it; then every target lies in the accumulator
+        if ((unsigned)(r3[0] + 1) <= (unsigned)(BR + 1) && (unsigned)(r3[1] + 1) <= (unsigned)(BR + 1) &&
+            (unsigned)(r3[2] + 1) <= (unsigned)(BZ + 1)) {
+          const int node[3] = {r3[0] + (oi[0] >= 0.5f ? 1 : 0), r3[1] + (oi[1] >= 0.5f ? 1 : 0),
+                               r3[2] + (oi[2] >= 0.5f ? 1 : 0)};
+          // trilinear targets node - 1 .. node meet the brick iff the node is in its node range
+          if ((unsigned)node[0] <= (unsigned)BR && (unsigned)node[1] <= (unsigned)BR &&
+              (unsigned)node[2] <= (unsigned)BZ)
+            deposit_trilinear<BR, BZ>(lo_f[0], hi_f[0], node, oi, scale[0]);
+          // faces r3 .. r3 + 1 along d, r3 across, meet the brick iff r3 is in [-1, B - 1]
+          if (ru_on && r3[0] < BR && r3[1] < BR && r3[2] < BZ) deposit_faces<BR, BZ>(&lo_f[1], &hi_f[1], r3, oi, ru, scale);
+        }
+      }
+      if (DO_NEW) {
+        const int r3[3] = {rel_local(ci_(cn), bx, G.n[0]), rel_local(cj_(cn), by, G.n[1]),
+                           rel_local(ck_(cn), bz, G.n[2])};
+        const int node[3] = {r3[0] + (on3[0] >= 0.5f ? 1 : 0), r3[1] + (on3[1] >= 0.5f ? 1 : 0),
+                             r3[2] + (on3[2] >= 0.5f ? 1 : 0)};
+        if ((unsigned)node[0] <= (unsigned)BR && (unsigned)node[1] <= (unsigned)BR && (unsigned)node[2] <= (unsigned)BZ)
+          deposit_trilinear<BR, BZ>(lo_f[FE], hi_f[FE], node, on3, rt * scale[4]);
+      }
     }
+    __syncthreads();
     if (tile) {
-      // split brick: the last slice writes the cells from the tile
+      // split brick: add this slice into the brick's global tile; the last slice writes the cells
+      for (int s = threadIdx.x; s < NF * NB; s += blockDim.x) {
+        const int q = s / NB, r = s % NB;
+        const int sl = q * SLOTS + Acc<BR, BZ>::slot(r % BR, (r / BR) % BR, r / (BR * BR));
+        const long long v = get_fixed(&acc_lo[sl], &acc_hi[sl]);
+        const int fld = DO_INT ? q : 4;
+        if (v) atomicAdd((unsigned long long *)&tile[fld * NB + r], (unsigned long long)v);
+      }
       __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) misc[33] = (atomicAdd(&w.done[slot_idx], 1) == nch - 1);
       __syncthreads();
       const int last = misc[33];
-      if (last) {
-        __threadfence();
-        long long tot[5] = {0, 0, 0, 0, 0};
-        for (int s = threadIdx.x; s < NB3; s += blockDim.x) {
-          const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
-          const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
-#pragma unroll
-          for (int fld = 0; fld < 5; ++fld) {
-            if (fld < 4 ? !DO_INT : !DO_NEW) continue;
-            const long long v = __ldcg(&tile[fld * NB3 + s]);
-            tile[fld * NB3 + s] = 0;  // ready for the next launch
-            const bool zero_ru = fld >= 1 && fld <= 3 && !twc;
-            outs[fld][g] = zero_ru ? 0.0 : fixed_to_f64(v, f.se[fld]);
-            tot[fld] += zero_ru ? 0 : v;
-          }
-        }
-        for (int fld = 0; fld < 5; ++fld) {
-          if (fld < 4 ? !DO_INT : !DO_NEW) continue;
-          const long long s = block_sum_i64(tot[fld], red);
-          if (threadIdx.x == 0 && s) atomicAdd(&totals[fld], (unsigned long long)s);
-        }
-        if (threadIdx.x == 0) w.done[slot_idx] = 0;
-      }
-      __syncthreads();
+      if (!last) continue;
+      __threadfence();
     }
+    long long tot[5] = {0, 0, 0, 0, 0};
+    for (int s = threadIdx.x; s < NB; s += blockDim.x) {
+      const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
+      const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
+      const int sl = Acc<BR, BZ>::slot(lx, ly, lz);
+#pragma unroll
+      for (int fld = 0; fld < 5; ++fld) {
+        if (fld < 4 ? !DO_INT : !DO_NEW) continue;
+        const int q = fld < 4 ? fld : FE;
+        long long v;
+        if (tile) {
+          v = __ldcg(&tile[fld * NB + s]);
+          tile[fld * NB + s] = 0;  // ready for the next launch
+        } else {
+          v = get_fixed(&lo_f[q][sl], &hi_f[q][sl]);
+        }
+        const bool zero_ru = fld >= 1 && fld <= 3 && !twc;  // RHS_RU = 0 without TWC (grid.cpp:671)
+        double *out = fld == 0 ? outC : (fld == 1 ? outX : (fld == 2 ? outY : (fld == 3 ? outZ : outE)));
+        out[g] = zero_ru ? 0.0 : fixed_to_f64(v, se[fld]);
+        tot[fld] += zero_ru ? 0 : v;
+      }
+    }
+#pragma unroll
+    for (int fld = 0; fld < 5; ++fld) {
+      if (fld < 4 ? !DO_INT : !DO_NEW) continue;
+      const long long sum = block_sum_i64(tot[fld], red);
+      if (threadIdx.x == 0 && sum) atomicAdd(&totals[fld], (unsigned long long)sum);
+    }
+    if (tile && threadIdx.x == 0) w.done[slot_idx] = 0;
+    __syncthreads();
   }
 }
 
@@ -1439,9 +1431,9 @@ int sort_step(pstep_ctx *h) {
     const int nbk = w.nbd;
     const int wblocks = (int)(((int64_t)nbk * 32 + kThreads - 1) / kThreads);  // one warp per brick
     if (w.br == 16)
-      k_work_count<16><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+      k_work_count<16, 8><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
     else
-      k_work_count<8><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+      k_work_count<8, 8><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
     PSTEP_LAUNCHED(h);
     TRY32(exclusive_scan(h, w.cnt_a, nbk, w.off_a, nullptr));
     TRY32(exclusive_scan(h, w.cnt_b, nbk, w.off_b, nullptr));
@@ -1498,17 +1490,19 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->sidx, cap));
   {  // deposit work list
     Work &w = f->work;
-    w.br = 16;
-    for (int d = 0; d < 3; ++d)
-      if (G.n[d] % 16 != 0 || G.n[d] < 32) w.br = 8;
-    const int64_t nbk = (int64_t)(G.n[0] / w.br) * (G.n[1] / w.br) * (G.n[2] / w.br);
+    // 16 x 16 x 8 where the grid allows (the window of a brick and two cells must not
+    // wrap onto itself), else 8 x 8 x 8
+    const bool big = G.n[0] % 16 == 0 && G.n[0] >= 32 && G.n[1] % 16 == 0 && G.n[1] >= 32 && G.n[2] >= 16;
+    w.br = big ? 16 : 8;
+    w.bz = 8;
+    const int64_t nbk = (int64_t)(G.n[0] / w.br) * (G.n[1] / w.br) * (G.n[2] / w.bz);
     w.nbd = (int)nbk;
     // a split brick's window holds more than kChunkMax particles and the windows
     // hold at most kVisit * cap particles in all
-    const int64_t visit = w.br == 16 ? DepTraits<16>::kVisit : DepTraits<8>::kVisit;
+    const int64_t visit = w.br == 16 ? DepTraits<16, 8>::kVisit : DepTraits<8, 8>::kVisit;
     w.slot_cap = visit * (int64_t)h->cap / kChunkMax + 1;
     w.err = h->err_word;
-    const int64_t br3 = (int64_t)w.br * w.br * w.br;
+    const int64_t br3 = (int64_t)w.br * w.br * w.bz;
     // items: one per unsplit brick plus ceil(window / kChunkMax) <= 2 window / kChunkMax
     // per split brick, so at most nbk + 2 * kVisit * cap / kChunkMax
     TRY32(dalloc32(h, w.items, (size_t)(nbk + 2 * w.slot_cap + 64)));
@@ -1766,6 +1760,7 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
   cd.dp_per_itth = (cfg.nu > 0 && cfg.k > 0) ? (float)(1.0 / (cfg.nu * kPi * cfg.k)) : 0.f;
   cd.dp = (float)cfg.dp;
   cd.idx = (float)G.idx[0];
+  h->corr_every_stage = pc->every_stage ? 1 : 0;
   for (int q = 0; q < 4; ++q) {
     if (!f.drive[q]) TRY32(dalloc32(h, f.drive[q], (size_t)h->cap));
     PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
@@ -1812,26 +1807,29 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
   F32Form &f = *h->f32;
   const C32 c = make_c32(h, k, pre, post);
   const int64_t n = h->np;
+  CorrDev cd = *reinterpret_cast<const CorrDev *>(h->corr_dev);
+  cd.wait_limit = h->wait_limit;
+  cd.idle_first = h->wait_idle ? 1u : 0u;
+  if (n > 0 && h->corr_on && (k == 0 || h->corr_every_stage)) {
+    // the network at this stage's x_int: persistent CTAs of two warpgroups, 4 per SM,
+    // tiles of 128 particles
+    prof_begin(h, PSTEP_PHASE_NETWORK);
+    const int64_t pairs = (n + 2 * corr::kRows - 1) / (2 * corr::kRows);
+    const unsigned grid = (unsigned)(pairs < 4 * (int64_t)h->num_sms ? pairs : 4 * (int64_t)h->num_sms);
+    auto net = k == 0 ? k_corr_net<0> : (k == 1 ? k_corr_net<1> : (k == 2 ? k_corr_net<2> : k_corr_net<3>));
+    // the shared-memory opt-in belongs to the current (launch) device: set it per launch
+    PSTEP_CUDA(cudaFuncSetAttribute(net, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr::kAlloc));
+    net<<<grid, corr::kThreads, corr::kAlloc, h->stream>>>(h->geom, f, c, n, h->err_word, cd);
+    PSTEP_LAUNCHED(h);
+    prof_end(h, PSTEP_PHASE_NETWORK);
+  }
   prof_begin(h, PSTEP_PHASE_ADVANCE);
   if (n > 0 && h->corr_on) {
-    CorrDev cd = *reinterpret_cast<const CorrDev *>(h->corr_dev);
-    cd.wait_limit = h->wait_limit;
-    cd.idle_first = h->wait_idle ? 1u : 0u;
-    if (k == 0) {
-      // the network: persistent CTAs of two warpgroups, 3 per SM, tiles of 128 particles
-      const int64_t pairs = (n + 2 * corr::kRows - 1) / (2 * corr::kRows);
-      const unsigned grid = (unsigned)(pairs < 3 * (int64_t)h->num_sms ? pairs : 3 * (int64_t)h->num_sms);
-      // the shared-memory opt-in belongs to the current (launch) device: set it per launch
-      PSTEP_CUDA(cudaFuncSetAttribute(k_advance32_mlp<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)corr::kAlloc));
-      k_advance32_mlp<0><<<grid, corr::kThreads, corr::kAlloc, h->stream>>>(h->geom, f, c, h->cfg.twc, n,
-                                                                            h->err_word, cd);
-    } else if (k == 1) {
-      k_advance32_corr<1><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd);
-    } else if (k == 2) {
-      k_advance32_corr<2><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd);
-    } else {
-      k_advance32_corr<3><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd);
+    switch (k) {
+      case 0: k_advance32_corr<0><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+      case 1: k_advance32_corr<1><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+      case 2: k_advance32_corr<2><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
+      default: k_advance32_corr<3><<<nb(n), 256, 0, h->stream>>>(h->geom, f, c, h->cfg.twc, n, h->err_word, cd); break;
     }
     PSTEP_LAUNCHED(h);
   } else if (n > 0) {
@@ -1852,33 +1850,33 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
 }
 
 namespace {
-// one launch of the deposit variant for (do_int, do_new) with brick edge BR:
+// one launch of the deposit variant for (do_int, do_new) with bricks BR x BR x BZ:
 // persistent CTAs (as many as fit on the SMs) pulling work items
-template <bool DO_INT, bool DO_NEW, int BR>
+template <bool DO_INT, bool DO_NEW, int BR, int BZ>
 int dep_run1(pstep_ctx *h, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z, double *E) {
-  constexpr int NF = DO_INT ? 4 : 1;  // fields of the widest pass
-  constexpr size_t smem = DepSmem<BR, NF>::kBytes;
-  auto kern = k_dep32<DO_INT, DO_NEW, BR>;
+  constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
+  constexpr size_t smem = DepSmem<BR, BZ, NF>::kBytes;
+  auto kern = k_dep32<DO_INT, DO_NEW, BR, BZ>;
   PSTEP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  PSTEP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, DepTraits<BR>::kThreads, smem));
+  PSTEP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, DepTraits<BR, BZ>::kThreads, smem));
   if (per_sm < 1) {
     snprintf(h->err, sizeof h->err, "deposit kernel does not fit on an SM (%zu B shared memory)", smem);
     return PSTEP_ERR_CUDA;
   }
   F32Form &f = *h->f32;
-  kern<<<h->num_sms * per_sm, DepTraits<BR>::kThreads, smem, h->stream>>>(h->geom, f, SI, SN, f.work, h->cfg.twc,
-                                                                           C, X, Y, Z, E, f.totals);
+  kern<<<h->num_sms * per_sm, DepTraits<BR, BZ>::kThreads, smem, h->stream>>>(h->geom, f, SI, SN, f.work,
+                                                                               h->cfg.twc, C, X, Y, Z, E, f.totals);
   PSTEP_LAUNCHED(h);
   return PSTEP_OK;
 }
 
-template <int BR>
+template <int BR, int BZ>
 int dep_run(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z,
             double *E) {
-  if (do_int && do_new) return dep_run1<true, true, BR>(h, SI, SN, C, X, Y, Z, E);
-  if (do_int) return dep_run1<true, false, BR>(h, SI, SN, C, X, Y, Z, E);
-  return dep_run1<false, true, BR>(h, SI, SN, C, X, Y, Z, E);
+  if (do_int && do_new) return dep_run1<true, true, BR, BZ>(h, SI, SN, C, X, Y, Z, E);
+  if (do_int) return dep_run1<true, false, BR, BZ>(h, SI, SN, C, X, Y, Z, E);
+  return dep_run1<false, true, BR, BZ>(h, SI, SN, C, X, Y, Z, E);
 }
 
 int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
@@ -1890,9 +1888,9 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   double *C = h->dep[PSTEP_FIELD_C], *X = h->dep[PSTEP_FIELD_RU_X], *Y = h->dep[PSTEP_FIELD_RU_Y],
          *Z = h->dep[PSTEP_FIELD_RU_Z], *E = h->dep[PSTEP_FIELD_PART_TEMP];
   if (f.work.br == 16) {
-    TRY32(dep_run<16>(h, do_int, do_new, SI, SN, C, X, Y, Z, E));
+    TRY32((dep_run<16, 8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E)));
   } else {
-    TRY32(dep_run<8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E));
+    TRY32((dep_run<8, 8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E)));
   }
   // interior values are final (periodic targets): refresh the ghost layers only
   if (do_int) {

@@ -165,7 +165,7 @@ def _temp_interp(spec: Spec, g, pos: np.ndarray) -> np.ndarray:
             (1 - tx) * (1 - ty) * (1 - tz) * T[nk - 1, nj - 1, ni - 1])
 
 
-def run_box(spec: Spec, run: dict, model: dict | None = None, record: bool = True) -> dict:
+def run_box(spec: Spec, run: dict, model: dict | None = None, record: bool = True, every_stage: bool = False) -> dict:
     """One quiescent box on the GPU; records, from step record_from on, the state at the start of
     each step and, for stage 0 (x_int = x), the gas values the particle update used (the kept
     values) and the plain interpolation -- the true disturbance. Without a model the two agree;
@@ -176,7 +176,7 @@ def run_box(spec: Spec, run: dict, model: dict | None = None, record: bool = Tru
     ps.load(*[np.ascontiguousarray(st[k]) for k in ("x", "y", "z", "u", "v", "w", "t", "flag")])
     ps.set_props(**props)
     if model is not None:
-        ps.set_correction(model, const["nu"])
+        ps.set_correction(model, const["nu"], every_stage=every_stage)
     g = gas.GasStep(gcfg, ps)
     z = np.zeros((spec.n,) * 3)
     g.init(z, z, z, np.ones((spec.n,) * 3), 1.0)
@@ -360,9 +360,10 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
 
 
 def evaluate(model: dict, spec: Spec | None = None, seed: int = 4001, lattice: int = 32, runs: int | None = None,
-             log=print) -> dict:
+             log=print, every_stage: bool = False) -> dict:
     """Plain against corrected step on held-out quiescent boxes (particles from the training
-    distributions, `lattice` spacing): RMS over the boxes of each error of `errors`."""
+    distributions, `lattice` spacing): RMS over the boxes of each error of `errors`.
+    every_stage: the network runs at every stage instead of once per step."""
     spec = spec or Spec()
     espec = dataclasses.replace(spec, lattice=lattice)
     held = sample(espec, seed)
@@ -371,7 +372,8 @@ def evaluate(model: dict, spec: Spec | None = None, seed: int = 4001, lattice: i
     res = {"plain": [], "corrected": []}
     per_box = []
     for r in pick:
-        e = {name: errors(espec, run_box(espec, held[r], m)) for name, m in (("plain", None), ("corrected", model))}
+        e = {name: errors(espec, run_box(espec, held[r], m, every_stage=every_stage))
+             for name, m in (("plain", None), ("corrected", model))}
         for name in res:
             res[name].append(e[name])
         per_box.append(dict(box=r, nu=held[r]["nu"], **{f"{n}_{k}": v for n in e for k, v in e[n].items()}))

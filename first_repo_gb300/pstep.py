@@ -45,7 +45,8 @@ class Props(C.Structure):
 
 class Correction(C.Structure):
     _fields_ = [("params", C.POINTER(C.c_float)), ("shift", C.c_float * 10), ("scale", C.c_float * 10),
-                ("lo", C.c_float * 4), ("hi", C.c_float * 4), ("prior_re", C.c_float), ("nu_gas", C.c_double)]
+                ("lo", C.c_float * 4), ("hi", C.c_float * 4), ("prior_re", C.c_float), ("nu_gas", C.c_double),
+                ("every_stage", C.c_int32)]
 
 
 class Config(C.Structure):
@@ -68,7 +69,7 @@ EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_pa
            "pstep_end_stage", "pstep_end_step", "pstep_run", "pstep_get_field", "pstep_energy_mean", "pstep_momentum_sums",
            "pstep_get_particle_array", "pstep_last_error", "pstep_status_string", "pstep_check",
            "pstep_last_run_ms", "pstep_launch_count", "pstep_profile", "pstep_profile_read"]
-PHASES = ["advance", "deposit_int", "order", "sort", "deposit_temp", "reorder"]
+PHASES = ["advance", "deposit_int", "order", "sort", "deposit_temp", "reorder", "network"]
 
 
 def lib():
@@ -223,9 +224,10 @@ class ParticleStep:
                 pr.accel[d] = addr(accel[d])
         self._ok(self.L.pstep_set_particle_props(self.h, C.byref(pr), int(on_dev or 0)))
 
-    def set_correction(self, model, nu_gas: float | None = None):
+    def set_correction(self, model, nu_gas: float | None = None, every_stage: bool = False):
         """Learned correction (pstep_set_correction): model = dict(params, shift, scale, lo, hi)
-        as made by first_repo_gb300.learn, nu_gas the gas kinematic viscosity; None: off."""
+        as made by first_repo_gb300.learn, nu_gas the gas kinematic viscosity; None: off.
+        every_stage: run the network at every stage (default: stage 0, output kept for the step)."""
         if model is None:
             self._ok(self.L.pstep_set_correction(self.h, None))
             return
@@ -239,6 +241,7 @@ class ParticleStep:
                 arr[i] = float(vals[i])
         c.prior_re = float(model.get("prior_re", 0.0))
         c.nu_gas = float(nu_gas if nu_gas is not None else model["nu_gas"])
+        c.every_stage = 1 if every_stage else 0
         self._ok(self.L.pstep_set_correction(self.h, C.byref(c)))
 
     def set_wait_limit(self, polls: int = 0, idle_first: bool = False):

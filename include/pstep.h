@@ -181,6 +181,9 @@ typedef struct pstep_correction {
                                 (d_p/dx) / (1 + Re_p / ((d_p/dx) prior_re)), the disturbance's
                                 dependence on size and cell Reynolds number; 0: no prior */
   double nu_gas;             /* kinematic viscosity of the gas */
+  int32_t every_stage;       /* 0: the network runs at stage 0 and its output serves the step's
+                                four stages (each with its own drive slip and prior); 1: it runs
+                                at every stage, at that stage's x_int */
 } pstep_correction;
 /* NULL switches the correction off */
 int pstep_set_correction(pstep_handle h, const pstep_correction *c);
@@ -281,6 +284,7 @@ enum {
   PSTEP_PHASE_SORT,            /* counting sort by node (CSR) */
   PSTEP_PHASE_DEPOSIT_TEMP,    /* energy deposit, fold, refresh, interior mean */
   PSTEP_PHASE_REORDER,         /* per-step reorder of particle storage */
+  PSTEP_PHASE_NETWORK,         /* FP32 learned correction: the tensor-core network */
   PSTEP_NUM_PHASES
 };
 int pstep_profile(pstep_handle h, int enable);

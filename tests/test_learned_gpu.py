@@ -7,7 +7,9 @@
 2. The library's training kernels fit quiescent-gas data.
 3. The quiescent-gas test: the committed network, trained on the quiescent-gas
    runs by the library's own kernels, against plain interpolation on held-out
-   boxes (thresholds in the test)."""
+   boxes (thresholds in the test).
+4. One inference per step (its output applied at the four stages with each stage's
+   own drive slip) against an inference at every stage, on held-out boxes."""
 import json
 import os
 
@@ -135,3 +137,19 @@ def test_quiescent_gas_correction(built_cuda):
     assert r["settle_reduction"] >= 5.0, summary
     assert r["temp_reduction"] >= 5.0, summary
     assert r["slip_reduction"] >= 2.4, summary
+
+
+def test_once_per_step_inference_matches_every_stage(built_cuda):
+    """The network once per step (the default, its output kept for stages 1-3) against the
+    network at every stage (at each stage's x_int, pstep_correction.every_stage), on four
+    held-out quiescent boxes: each error's RMS agrees within 5% of the plain step's error,
+    i.e. reusing the output changes the correction's accuracy by a small fraction of what
+    the correction gains."""
+    model = learn.load_model()
+    once = learn.evaluate(model, runs=4, log=lambda *a: None)
+    every = learn.evaluate(model, runs=4, log=lambda *a: None, every_stage=True)
+    report = {k: {"once": once["corrected"][k], "every": every["corrected"][k], "plain": once["plain"][k]}
+              for k in ("slip_rms", "settle_rms", "temp_rms")}
+    print("inference once per step vs every stage:", json.dumps(report))
+    for k, v in report.items():
+        assert abs(v["once"] - v["every"]) <= 0.05 * v["plain"], (k, v)
