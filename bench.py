@@ -508,22 +508,19 @@ def main():
         hout = [pinned_like(a) for a in arrs]
         hf = [pinned_like(f) for f in fields]
         out_f = [pinned_like(np.empty_like(fields[0])) for _ in range(5)]
-        names = ["x", "y", "z", "u", "v", "w", "T", "flag"]
         import ctypes as C
         L = pstep.lib()
         bufs = [hin, hout]
 
         def one_step():
+            # (the correction set above persists across uploads; an upload clears its drive state)
             src, dst = bufs
             g.load(*src)
-            if corr_model is not None:
-                g.set_correction(corr_model, nu_gas)
             g.bind_velocity(*hf[:3])
             g.bind_temperature(hf[3])
             g.prime()
             g.run(1)
-            for i, nm in enumerate(names):
-                g._ok(L.pstep_get_particle_array(g.h, pstep.ARRAY_IDS[nm], dst[i].ctypes.data, 0))
+            g.download(*dst)
             for i, fname in enumerate(pstep.FIELD_IDS):
                 g._ok(L.pstep_get_field(g.h, pstep.FIELD_IDS[fname], out_f[i].ctypes.data, 0))
             bufs.reverse()

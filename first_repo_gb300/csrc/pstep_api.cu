@@ -371,6 +371,16 @@ int pstep_upload_particles(pstep_handle h, int64_t n, const double *x, const dou
   return PSTEP_OK;
 }
 
+int pstep_download_particles(pstep_handle h, double *x, double *y, double *z, double *u, double *v, double *w,
+                             double *t, int32_t *flag, int on_device) {
+  if (!h) return PSTEP_ERR_ARG;
+  if (h->np > 0 && (!x || !y || !z || !u || !v || !w || !t || !flag)) return fail(h, PSTEP_ERR_ARG, "null array");
+  double *dst[7] = {x, y, z, u, v, w, t};
+  if (is_f32(h)) return pstep::f32_download(h, dst, flag, on_device);
+  for (int q = 0; q < 7; ++q) TRY(pstep_get_particle_array(h, PSTEP_X + q, dst[q], on_device));
+  return pstep_get_particle_array(h, PSTEP_FLAG, flag, on_device);
+}
+
 int pstep_set_tau_p(pstep_handle h, const double *tau, int on_device) {
   if (!h) return PSTEP_ERR_ARG;
   if (is_f32(h)) return f32_set_tau(h, tau, on_device);

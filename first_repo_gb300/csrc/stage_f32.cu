@@ -1953,6 +1953,69 @@ int f32_positions(pstep_ctx *h, const int32_t *idx, int32_t n, double *xyz) {
   return PSTEP_OK;
 }
 
+namespace {
+// the base state of particles p0 .. p0 + n - 1 as fp64 (absolute positions, velocities,
+// temperature) into dst[q][0 .. n): the arrays pstep_get_particle_array returns for
+// PSTEP_X .. PSTEP_T, all seven from one read of each particle
+__global__ void k_to_f64_all(Geom G, Set32 S, double tref, int64_t p0, int64_t n, double *__restrict__ x,
+                             double *__restrict__ y, double *__restrict__ z, double *__restrict__ u,
+                             double *__restrict__ v, double *__restrict__ w, double *__restrict__ t) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int64_t p = p0 + q;
+  const uint32_t c = S.cell[p];
+  x[q] = ((double)ci_(c) + (double)S.o[0][p]) * (G.l[0] / G.n[0]);
+  y[q] = ((double)cj_(c) + (double)S.o[1][p]) * (G.l[1] / G.n[1]);
+  z[q] = ((double)ck_(c) + (double)S.o[2][p]) * (G.l[2] / G.n[2]);
+  u[q] = (double)S.v[0][p];
+  v[q] = (double)S.v[1][p];
+  w[q] = (double)S.v[2][p];
+  t[q] = (double)S.v[3][p] + tref;
+}
+}  // namespace
+
+// pstep_download_particles, FP32 form: the base state and the ids in storage order. Host
+// destinations: chunks converted into the two staging slots in turn and copied out on the
+// copy stream, all seven arrays per chunk, so one pipeline serves the whole download.
+int f32_download(pstep_ctx *h, double *const dst[7], int32_t *flag, int on_device) {
+  F32Form &f = *h->f32;
+  const int64_t n = h->np;
+  if (n == 0) return PSTEP_OK;
+  const Set32 &B = f.set[SBASE];
+  if (on_device) {
+    k_to_f64_all<<<nb(n), kThreads, 0, h->stream>>>(h->geom, B, f.tref, 0, n, dst[0], dst[1], dst[2], dst[3],
+                                                    dst[4], dst[5], dst[6]);
+    PSTEP_LAUNCHED(h);
+    PSTEP_CUDA(cudaMemcpyAsync(flag, h->s.flag, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, h->stream));
+    PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+    return PSTEP_OK;
+  }
+  TRY32(stage_init(h));
+  for (int64_t c = 0, p0 = 0; p0 < n; ++c, p0 += kStageChunk) {
+    const int sl = (int)(c & 1);
+    const int64_t len = n - p0 < kStageChunk ? n - p0 : kStageChunk;
+    double *b = f.stage[sl];
+    PSTEP_CUDA(cudaStreamWaitEvent(h->stream, f.ev_copied[sl], 0));  // the slot's last copy (any call) is done
+    k_to_f64_all<<<nb(len), kThreads, 0, h->stream>>>(h->geom, B, f.tref, p0, len, b, b + kStageChunk,
+                                                      b + 2 * kStageChunk, b + 3 * kStageChunk, b + 4 * kStageChunk,
+                                                      b + 5 * kStageChunk, b + 6 * kStageChunk);
+    PSTEP_LAUNCHED(h);
+    PSTEP_CUDA(cudaEventRecord(f.ev_used[sl], h->stream));
+    PSTEP_CUDA(cudaStreamWaitEvent(f.copy_stream, f.ev_used[sl], 0));
+    for (int q = 0; q < 7; ++q)
+      PSTEP_CUDA(cudaMemcpyAsync(dst[q] + p0, b + q * kStageChunk, sizeof(double) * len, cudaMemcpyDeviceToHost,
+                                 f.copy_stream));
+    PSTEP_CUDA(cudaEventRecord(f.ev_copied[sl], f.copy_stream));
+  }
+  // the ids need no conversion: one copy behind the chunks, after everything enqueued on
+  // the handle's stream so far
+  PSTEP_CUDA(cudaEventRecord(f.ev_used[0], h->stream));
+  PSTEP_CUDA(cudaStreamWaitEvent(f.copy_stream, f.ev_used[0], 0));
+  PSTEP_CUDA(cudaMemcpyAsync(flag, h->s.flag, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, f.copy_stream));
+  PSTEP_CUDA(cudaStreamSynchronize(f.copy_stream));
+  return PSTEP_OK;
+}
+
 int f32_get_array(pstep_ctx *h, int id, void *dst, int on_device) {
   F32Form &f = *h->f32;
   const int64_t n = h->np;

@@ -272,13 +272,23 @@ def prior(f: np.ndarray) -> np.ndarray:
     return dpdx / (1.0 + np.exp(f[:, 7]) / dpdx / PRIOR_RE)
 
 
-def train(f: np.ndarray, y: np.ndarray, steps: int = 20000, batch: int = 8192, lr: float = 1e-3, seed: int = 0):
+def train(f: np.ndarray, y: np.ndarray, steps: int = 20000, batch: int = 8192, lr: float = 1e-3, seed: int = 0,
+          emphasis: float = 0.0):
+    """Adam on the mean squared error of the targets in units of the prior. emphasis > 0 draws
+    the training rows with probability proportional to prior ** emphasis (seeded), so that the
+    particles with the largest disturbance per unit slip -- whose error dominates the
+    self-induced slip error -- weigh more."""
     shift, scale, lo, hi = normaliser(f)
+    pr = prior(f)
+    if emphasis > 0:
+        w = pr ** emphasis
+        pick = np.random.default_rng(seed + 17).choice(len(f), size=len(f), p=w / w.sum())
+        f, y, pr = f[pick], y[pick], pr[pick]
     x = ((f - shift) * scale).astype(np.float32)
     net = mlp.Mlp(seed=seed)
     # targets in units of the prior; a few samples with a near-zero drive temperature
     # difference give meaningless ratios, which are clipped
-    yt = np.clip(y / prior(f)[:, None], -TARGET_CLIP, TARGET_CLIP)
+    yt = np.clip(y / pr[:, None], -TARGET_CLIP, TARGET_CLIP)
     net.set_data(x, yt.astype(np.float32))
     loss = net.train(steps, batch=batch, lr=lr, seed=seed + 1)
     model = dict(params=net.params, shift=shift.astype(np.float32), scale=scale.astype(np.float32),
@@ -306,6 +316,51 @@ def errors(spec: Spec, rec: dict) -> dict:
                 temp_rms=float(np.sqrt(np.mean(e_t ** 2))))
 
 
+K_BINS = (0.0, 0.1, 0.3, 0.6, 0.9, float("inf"))
+
+
+def per_particle_slip(rec: dict) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Per particle id of a recorded run: the RMS over its samples of the self-induced slip
+    error (|gas velocity used| / terminal slip, as `errors`), and its mean K = |gas velocity
+    used| / |drive slip| (the disturbance per unit slip; meaningful in a plain run, where the
+    gas used is the disturbance itself)."""
+    c = rec["const"]
+    fl = rec["flag"]
+    gasv = np.stack([rec["ug"], rec["vg"], rec["wg"]], axis=1)
+    up = np.stack([rec["u"], rec["v"], rec["w"]], axis=1)
+    g = np.linalg.norm(gasv, axis=1)
+    s0 = np.linalg.norm(c["slip0"][fl], axis=1)
+    sd = np.linalg.norm(up - gasv, axis=1)
+    ids = np.unique(fl)
+    e2 = np.bincount(fl, weights=(g / s0) ** 2, minlength=ids.max() + 1)
+    k = np.bincount(fl, weights=np.where(sd > 0, g / np.maximum(sd, 1e-300), 0.0), minlength=ids.max() + 1)
+    cnt = np.bincount(fl, minlength=ids.max() + 1)
+    return ids, np.sqrt(e2[ids] / cnt[ids]), k[ids] / cnt[ids]
+
+
+def slip_by_k(pairs: list[tuple[dict, dict]]) -> list[dict]:
+    """Self-induced slip error of plain and corrected runs of the same particles, binned by
+    the particle's K (from its plain run): RMS per bin and the reduction."""
+    ep, ec, kk = [], [], []
+    for plain, corr in pairs:
+        ids_p, e_p, k_p = per_particle_slip(plain)
+        ids_c, e_c, _ = per_particle_slip(corr)
+        _, ip, ic = np.intersect1d(ids_p, ids_c, return_indices=True)
+        ep.append(e_p[ip])
+        ec.append(e_c[ic])
+        kk.append(k_p[ip])
+    ep, ec, kk = np.concatenate(ep), np.concatenate(ec), np.concatenate(kk)
+    out = []
+    for lo, hi in zip(K_BINS[:-1], K_BINS[1:]):
+        m = (kk >= lo) & (kk < hi)
+        if not m.any():
+            continue
+        p, c = float(np.sqrt(np.mean(ep[m] ** 2))), float(np.sqrt(np.mean(ec[m] ** 2)))
+        out.append(dict(k_lo=lo, k_hi=hi, particles=int(m.sum()), plain=p, corrected=c,
+                        reduction=p / max(c, 1e-300)))
+    return out
+
+
 def save_model(model: dict, path: str = MODEL_FILE, meta: dict | None = None):
     os.makedirs(os.path.dirname(path), exist_ok=True)
     np.savez(path, **{k: np.asarray(v) for k, v in model.items()}, meta=json.dumps(meta or {}))
@@ -318,7 +373,7 @@ def load_model(path: str = MODEL_FILE) -> dict:
 
 def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, eval_runs: int | None = None,
              steps: int = 20000, batch: int = 8192, lr: float = 1e-3, eval_lattice: int = 32, rounds: int = 2,
-             log=print) -> dict:
+             emphasis: float = 0.0, log=print) -> dict:
     """Generate the training set, train, and compare plain and corrected steps on held-out boxes.
 
     Data: the plain two-way-coupled runs, then `rounds` times the same boxes run with the
@@ -341,7 +396,7 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
     net_model = None
     for rnd in range(rounds):
         net_model, loss1, _ = train(np.concatenate(f_all), np.concatenate(y_all), steps=steps // 2, batch=batch, lr=lr,
-                                    seed=seed + 100 * rnd)
+                                    seed=seed + 100 * rnd, emphasis=emphasis)
         log(f"round {rnd} network: loss {loss1[-100:].mean():.4e}")
         for r, run in enumerate(runs):
             f, y, _ = raw_features(spec, run_box(spec, run, net_model))
@@ -350,7 +405,7 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
         log(f"round {rnd}: closed-loop samples from {len(runs)} boxes")
     f = np.concatenate(f_all)
     y = np.concatenate(y_all)
-    model, loss, net = train(f, y, steps=steps, batch=batch, lr=lr, seed=seed + 7)
+    model, loss, net = train(f, y, steps=steps, batch=batch, lr=lr, seed=seed + 7, emphasis=emphasis)
     log(f"trained: loss {loss[:10].mean():.4e} -> {loss[-100:].mean():.4e}")
     out = evaluate(model, spec, eval_seed, eval_lattice, eval_runs, log)
     out["samples"] = int(len(f))
@@ -371,9 +426,12 @@ def evaluate(model: dict, spec: Spec | None = None, seed: int = 4001, lattice: i
                                                     for i in range(runs)]
     res = {"plain": [], "corrected": []}
     per_box = []
+    pairs = []
     for r in pick:
-        e = {name: errors(espec, run_box(espec, held[r], m, every_stage=every_stage))
-             for name, m in (("plain", None), ("corrected", model))}
+        recs = {name: run_box(espec, held[r], m, every_stage=every_stage)
+                for name, m in (("plain", None), ("corrected", model))}
+        pairs.append((recs["plain"], recs["corrected"]))
+        e = {name: errors(espec, rec) for name, rec in recs.items()}
         for name in res:
             res[name].append(e[name])
         per_box.append(dict(box=r, nu=held[r]["nu"], **{f"{n}_{k}": v for n in e for k, v in e[n].items()}))
@@ -385,6 +443,7 @@ def evaluate(model: dict, spec: Spec | None = None, seed: int = 4001, lattice: i
     out["settle_reduction"] = out["plain"]["settle_rms"] / max(out["corrected"]["settle_rms"], 1e-300)
     out["temp_reduction"] = out["plain"]["temp_rms"] / max(out["corrected"]["temp_rms"], 1e-300)
     out["boxes"] = per_box
+    out["slip_by_k"] = slip_by_k(pairs)
     return out
 
 

@@ -63,7 +63,7 @@ _D = C.POINTER(C.c_double)
 _VP = C.c_void_p
 _H = C.c_void_p
 
-EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_set_tau_p", "pstep_set_particle_props", "pstep_set_correction", "pstep_set_wait_limit",
+EXPORTS = ["pstep_create", "pstep_destroy", "pstep_set_stream", "pstep_update_params", "pstep_upload_particles", "pstep_download_particles", "pstep_set_tau_p", "pstep_set_particle_props", "pstep_set_correction", "pstep_set_wait_limit",
            "pstep_num_particles", "pstep_bind_velocity", "pstep_bind_temperature", "pstep_prime",
            "pstep_stage_interp_advance_deposit", "pstep_wrap", "pstep_stage_temp", "pstep_stage",
            "pstep_end_stage", "pstep_end_step", "pstep_run", "pstep_get_field", "pstep_energy_mean", "pstep_momentum_sums",
@@ -82,6 +82,7 @@ def lib():
     L.pstep_update_params.argtypes = [_H, C.POINTER(Config)]
     L.pstep_upload_particles.argtypes = [_H, C.c_int64] + [_VP] * 8 + [C.c_int]
     L.pstep_set_tau_p.argtypes = [_H, _VP, C.c_int]
+    L.pstep_download_particles.argtypes = [_H] + [_VP] * 8 + [C.c_int]
     L.pstep_set_particle_props.argtypes = [_H, C.POINTER(Props), C.c_int]
     L.pstep_set_correction.argtypes = [_H, C.POINTER(Correction)]
     L.pstep_set_wait_limit.argtypes = [_H, C.c_uint32, C.c_int]
@@ -186,6 +187,11 @@ class ParticleStep:
         n = len(flag) if isinstance(flag, np.ndarray) else int(flag.numel())
         self._keep = [x, y, z, u, v, w, t, flag]
         self._ok(self.L.pstep_upload_particles(self.h, n, *[p for p, _ in ps], on_dev))
+
+    def download(self, x, y, z, u, v, w, t, flag):
+        """the base state and ids into preallocated arrays (pstep_download_particles)"""
+        ps = [_ptr(a) for a in (x, y, z, u, v, w, t, flag)]
+        self._ok(self.L.pstep_download_particles(self.h, *[p for p, _ in ps], ps[0][1]))
 
     def set_tau_p(self, tau):
         if tau is None:

@@ -136,6 +136,12 @@ int pstep_update_params(pstep_handle h, const pstep_config *cfg);
 int pstep_upload_particles(pstep_handle h, int64_t n, const double *x, const double *y, const double *z,
                            const double *u, const double *v, const double *w, const double *t,
                            const int32_t *flag, int on_device);
+/* Read the base particle state x,u,T and the ids back (the reference's public vectors
+ * after grid::TimeAdvance, grid.cpp:315-325): the same arrays as pstep_get_particle_array
+ * with PSTEP_X .. PSTEP_T and PSTEP_FLAG, in the same order, from one pass over the
+ * particles. Host destinations are complete when the call returns. */
+int pstep_download_particles(pstep_handle h, double *x, double *y, double *z, double *u, double *v, double *w,
+                             double *t, int32_t *flag, int on_device);
 /* Optional per-particle momentum relaxation time (same order as the upload);
  * replaces the scalar Tp for every particle. NULL restores the scalar. */
 int pstep_set_tau_p(pstep_handle h, const double *tau_p, int on_device);

@@ -80,3 +80,26 @@ def test_committed_network_file(tmp_path):
     back = learn.load_model(path)
     for k in model:
         assert np.array_equal(np.asarray(back[k]), np.asarray(model[k])), k
+
+
+def test_slip_error_binned_by_k():
+    """slip_by_k: per-particle RMS of |gas used| / terminal slip, binned by the particle's K from
+    the plain run (|gas| / |drive slip|); a correction removing 90% of every disturbance
+    reduces every bin 10x."""
+    rng = np.random.default_rng(0)
+    n, steps = 60, 3
+    fl = np.tile(np.arange(n), steps)
+    slip0 = rng.normal(size=(n, 3))
+    k = rng.uniform(0.0, 1.2, n)
+
+    def rec(scale):
+        g = slip0[fl] * scale[fl, None]
+        u = slip0[fl] + g
+        return dict(const=dict(slip0=slip0), flag=fl, ug=g[:, 0], vg=g[:, 1], wg=g[:, 2],
+                    u=u[:, 0], v=u[:, 1], w=u[:, 2])
+
+    bins = learn.slip_by_k([(rec(k), rec(0.1 * k))])
+    assert sum(b["particles"] for b in bins) == n
+    for b in bins:
+        assert abs(b["reduction"] - 10.0) < 1e-9
+        assert b["k_lo"] <= b["plain"] < max(b["k_hi"], 2.0)

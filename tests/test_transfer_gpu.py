@@ -66,3 +66,37 @@ def test_fp32_back_to_back_host_uploads(built_cuda):
     d = (g.array("x") - x + L / 2) % L - L / 2
     assert np.max(np.abs(d)) <= dx * 2.0 ** -23
     g.close()
+
+
+@pytest.mark.parametrize("form", [pstep.FP32, pstep.FP64])
+def test_download_particles_equals_the_array_reads(built_cuda, form):
+    """pstep_download_particles (one pass over every chunk, all arrays) returns exactly what
+    pstep_get_particle_array returns for PSTEP_X .. PSTEP_T and PSTEP_FLAG, into host and
+    into device memory, after a step (over three staging chunks for the FP32 form)."""
+    torch = pytest.importorskip("torch")
+    n = 64
+    count = 2 * STAGE_CHUNK + 4321 if form == pstep.FP32 else 50000
+    bp = helpers.make_bp(n, count)
+    rng = np.random.default_rng(13)
+    x, y, z = (rng.uniform(0.0, bp.l, count) for _ in range(3))
+    u, v, w = (rng.normal(0.0, 1.0, count) for _ in range(3))
+    t = rng.uniform(0.9, 1.1, count)
+    flag = rng.permutation(count).astype(np.int32)
+    g = pstep.ParticleStep(bp.step_config(), count, form, pstep.TRACK_ORDER if form == pstep.FP64 else 0)
+    g.load(x, y, z, u, v, w, t, flag)
+    zf = np.zeros((n + 2,) * 3)
+    g.bind_velocity(zf, zf, zf)
+    g.bind_temperature(zf + 1.0)
+    g.prime()
+    g.run(1)
+    names = ["x", "y", "z", "u", "v", "w", "T", "flag"]
+    want = [g.array(k) for k in names]
+    host = [np.empty(count, dtype=np.int32 if k == "flag" else np.float64) for k in names]
+    g.download(*host)
+    for k, a, b in zip(names, host, want):
+        assert helpers.bits_equal(a, b), k
+    dev = [torch.empty(count, dtype=torch.int32 if k == "flag" else torch.float64, device="cuda") for k in names]
+    g.download(*dev)
+    for k, a, b in zip(names, dev, want):
+        assert helpers.bits_equal(a.cpu().numpy(), b), k
+    g.close()
