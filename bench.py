@@ -190,38 +190,53 @@ def pinned_like(a: np.ndarray) -> np.ndarray:
 
 def fp32_error_report(g32, g64, L: float, n_cells: int) -> dict:
     """The FP32 form's error against the FP64 step run on the same inputs for the same
-    number of steps, matched by particle id and computed on the device:
-      position_cells_max       max over particles of |x32 - x64| (periodic) in cell units
-      velocity_rel_max / _p999 per particle |u32 - u64| / |u64| (velocity vectors)
-      temperature_rel_max      per particle |T32 - T64| / |T64|
-      rhs_t_rel_to_max         max |RHS_T32 - RHS_T64| / max |RHS_T64|
-      fields                   per deposited field max |f32 - f64| / max |f64| (C: interior)
-      energy_mean_rel          |mean32 - mean64| / |mean64|
-      momentum_rel_to_abs      per component |sum32 - sum64| / sum |RHS_RU64| over the interior
+    number of steps, matched by particle id and computed on the device.
+
+    Per particle, `*_max` is the largest error and `*_bulk` the largest over all but a
+    fraction 1e-6 of the particles: the reference's face-normal interpolation
+    (particle.cpp:340-360) is piecewise constant across the other two axes, so a particle
+    whose stage position lies within the fp32 resolution of a cell face (about 1e-7 cells)
+    can take the neighbouring cell's transverse velocity in one form and not the other, an
+    O(dx |grad u|) difference for that particle; `*_count` counts particles beyond 1e-5.
+      position_cells            |x32 - x64| (periodic) in cell units
+      velocity_rel              |u32 - u64| / |u64| (velocity vectors)
+      temperature_rel           |T32 - T64| / |T64|
+      rhs_t_rel_to_max          |RHS_T32 - RHS_T64| / max |RHS_T64|
+      fields                    per deposited field max |f32 - f64| / max |f64| (C: interior)
+      fields_l2                 per deposited field ||f32 - f64|| / ||f64|| over the interior
+      energy_mean_rel           |mean32 - mean64| / |mean64|
+      momentum_rel_to_abs       per component |sum32 - sum64| / sum |RHS_RU64| over the interior
     """
     import torch
     dev = "cuda"
     n = g32.np
     if g64.np != n:
         raise ValueError("populations differ in size")
+    k_out = max(1, int(1e-6 * n))
 
     def arr(g, name, dtype=torch.float64):
         t = torch.empty(n, dtype=dtype, device=dev)
         g.array(name, out=t)
         return t
 
+    def stats(name, e, rep):
+        rep[name + "_max"] = float(e.max())
+        rep[name + "_bulk"] = float(torch.topk(e, k_out + 1).values[-1])
+        rep[name + "_count"] = int((e > 1e-5).sum())
+
     i32 = torch.argsort(arr(g32, "flag", torch.int32))
     i64 = torch.argsort(arr(g64, "flag", torch.int32))
     if not torch.equal(arr(g32, "flag", torch.int32)[i32], arr(g64, "flag", torch.int32)[i64]):
         raise ValueError("particle ids differ")
-    rep = {}
+    rep = {"particles": n, "bulk_excludes": k_out}
     dx = L / n_cells
-    pos = 0.0
+    pos = torch.zeros(n, dtype=torch.float64, device=dev)
     for k in ("x", "y", "z"):
         d = arr(g32, k)[i32] - arr(g64, k)[i64]
         d = torch.remainder(d + L / 2, L) - L / 2
-        pos = max(pos, float(d.abs().max()) / dx)
-    rep["position_cells_max"] = pos
+        pos = torch.maximum(pos, d.abs() / dx)
+    stats("position_cells", pos, rep)
+    del pos
     du = torch.zeros(n, dtype=torch.float64, device=dev)
     sp = torch.zeros(n, dtype=torch.float64, device=dev)
     for k in ("u", "v", "w"):
@@ -229,18 +244,15 @@ def fp32_error_report(g32, g64, L: float, n_cells: int) -> dict:
         du += (a - b) ** 2
         sp += b ** 2
         del a, b
-    rel = torch.sqrt(du) / torch.sqrt(sp).clamp_min(1e-300)
-    rep["velocity_rel_max"] = float(rel.max())
-    rep["velocity_rel_p999"] = float(torch.quantile(rel[torch.randperm(n, device=dev)[: 1 << 22]], 0.999))
-    del du, sp, rel
+    stats("velocity_rel", torch.sqrt(du) / torch.sqrt(sp).clamp_min(1e-300), rep)
+    del du, sp
     a, b = arr(g32, "T")[i32], arr(g64, "T")[i64]
-    rep["temperature_rel_max"] = float(((a - b).abs() / b.abs().clamp_min(1e-300)).max())
+    stats("temperature_rel", (a - b).abs() / b.abs().clamp_min(1e-300), rep)
     a, b = arr(g32, "RHS_T")[i32], arr(g64, "RHS_T")[i64]
-    rep["rhs_t_rel_to_max"] = float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+    stats("rhs_t_rel_to_max", (a - b).abs() / b.abs().max().clamp_min(1e-300), rep)
     del a, b
     g = n_cells + 2
-    fields = {}
-    mom = {}
+    fields, fields_l2, mom = {}, {}, {}
     s32, s64 = g32.momentum_sums(), g64.momentum_sums()
     for i, name in enumerate(("C", "RHS_RU_x", "RHS_RU_y", "RHS_RU_z", "RHS_Part_Temp")):
         a = torch.empty(g ** 3, dtype=torch.float64, device=dev)
@@ -250,10 +262,12 @@ def fp32_error_report(g32, g64, L: float, n_cells: int) -> dict:
         a = a.view(g, g, g)[1:-1, 1:-1, 1:-1]
         b = b.view(g, g, g)[1:-1, 1:-1, 1:-1]
         fields[name] = float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+        fields_l2[name] = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b).clamp_min(1e-300))
         if 1 <= i <= 3:
             mom[name] = abs(s32[i - 1] - s64[i - 1]) / max(float(b.abs().sum()), 1e-300)
         del a, b
     rep["fields"] = fields
+    rep["fields_l2"] = fields_l2
     rep["momentum_rel_to_abs"] = mom
     e32, e64 = g32.energy_mean(), g64.energy_mean()
     rep["energy_mean_rel"] = abs(e32 - e64) / max(abs(e64), 1e-300)

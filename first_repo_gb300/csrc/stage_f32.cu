@@ -55,14 +55,13 @@ struct Set32 {
   float *v[4];  // u v w T
 };
 
-// Deposit bricks (the cells one CTA owns) are BR x BR x BZ: 16 x 16 x 8 where the
-// grid allows (x and y sides multiples of 16 and at least 32 cells, z a multiple of 8
-// and at least 16: a source window of the brick and two cells around it must not
-// wrap onto itself), else 8 x 8 x 8. A brick's source particles (those whose
-// step-start cell lies within two cells of it) are visited about
-// (BR+4)^2 (BZ+4) / (BR^2 BZ) times each: 2.34 for 16 x 16 x 8, 3.4 for 8^3. The
-// 16 x 16 x 8 shape keeps the five fields' accumulators (brick plus one cell) in the
-// shared memory of one CTA, so one walk deposits all of them.
+// Deposit bricks (the cells one CTA owns) are BR x BR x BZ = 16^3 where the grid
+// allows (every side a multiple of 16 and at least 32 cells: the source window of
+// the brick and two cells around it must not wrap onto itself), else 8^3. A
+// brick's source particles (those whose step-start cell lies within two cells of
+// it) are visited about (BR+4)^2 (BZ+4) / (BR^2 BZ) times each: 1.95 at 16^3, 3.4 at
+// 8^3. Every contribution is added once, by the brick that holds its target: the
+// shared-memory adds, not the visits, bound the kernel.
 //
 // Work list of the deposit: one item per deposit brick, or -- for bricks whose
 // source window holds more than kChunkMax particles -- several items, each a
@@ -74,8 +73,8 @@ template <int BR, int BZ> struct DepTraits;
 template <> struct DepTraits<8, 8> {
   static constexpr int kThreads = 256, kVisit = 4;  // (12/8)^3 = 3.4
 };
-template <> struct DepTraits<16, 8> {
-  static constexpr int kThreads = 1024, kVisit = 3;  // (20/16)^2 (12/8) = 2.34
+template <> struct DepTraits<16, 16> {
+  static constexpr int kThreads = 1024, kVisit = 2;  // (20/16)^3 = 1.95
 };
 
 struct Work {
@@ -88,7 +87,7 @@ struct Work {
   int32_t *done;        // per slot: items finished
   long long *tiles;     // per slot: 5 x BR^2 BZ int64
   int64_t slot_cap;
-  int br, bz;           // deposit brick edges: 16 x 16 x 8 or 8 x 8 x 8
+  int br, bz;           // deposit brick edges: 16^3 or 8^3
   int nbd;              // number of deposit bricks
   int32_t *err;         // device error word (kErrCapacity)
 };
@@ -812,16 +811,11 @@ __device__ __forceinline__ long long get_fixed(const uint32_t *lo, const uint32_
   return (long long)(int32_t)*hi * 65536ll + (long long)*lo;
 }
 
-// Accumulator of a deposit brick: its BR x BR x BZ cells and one cell around them,
-// brick-relative x, y in [-1, BR], z in [-1, BZ], rows padded by one word so that
-// neighbouring rows do not fall on the same shared-memory banks. A particle whose
-// every target lies in this region adds without a per-target test; what lands in
-// the outer layer is not read (the neighbouring brick counts it for its own cells).
+// Accumulator of a deposit brick: its BR x BR x BZ cells, rows padded by one word so
+// that neighbouring rows do not fall on the same shared-memory banks.
 template <int BR, int BZ> struct Acc {
-  static constexpr int kSideY = BR + 2, kSideZ = BZ + 2, kRow = BR + 3, kSlots = kRow * kSideY * kSideZ;
-  static __device__ __forceinline__ int slot(int x, int y, int z) {
-    return ((z + 1) * kSideY + (y + 1)) * kRow + (x + 1);
-  }
+  static constexpr int kRow = BR + 1, kSlots = kRow * BR * BZ;
+  static __device__ __forceinline__ int slot(int x, int y, int z) { return (z * BR + y) * kRow + x; }
 };
 
 // The source window of the deposit brick at (bx, by, bz) -- its cells and two
@@ -904,19 +898,25 @@ __global__ void k_work_fill(Work w, int nb) {
 }
 
 // trilinear deposit (particle.cpp:526-559, :586-658) of a particle with in-cell offsets
-// o3 whose round() node is `node` (brick-relative, in [0, BR] x [0, BR] x [0, BZ]) and
-// value `val` (already times the field's fixed-point scale): the 8 cells node - 1 ..
-// node get products of x_l / (1 - x_l), all inside the accumulator region
+// o3 whose round() node is `node` (brick-relative) and value `val` (already times the
+// field's fixed-point scale): of the 8 cells node - 1 .. node, which get products of
+// x_l / (1 - x_l), those inside the brick are added (the others belong to the
+// neighbouring bricks, which add them themselves); lanes with no target there issue
+// no shared-memory access for it
 template <int BR, int BZ>
 __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, const int node[3], const float o3[3],
                                                   float val) {
   using A = Acc<BR, BZ>;
   float w[3][2];
+  bool ok[3][2];
+  const int ext[3] = {BR, BR, BZ};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float xl = o3[d] - (o3[d] >= 0.5f ? 1.f : 0.f) + 0.5f;
     w[d][0] = 1.f - xl;  // cell node - 1
     w[d][1] = xl;        // cell node
+    ok[d][0] = (unsigned)(node[d] - 1) < (unsigned)ext[d];
+    ok[d][1] = (unsigned)node[d] < (unsigned)ext[d];
   }
   const int base = A::slot(node[0] - 1, node[1] - 1, node[2] - 1);
 #pragma unroll
@@ -924,28 +924,37 @@ __device__ __forceinline__ void deposit_trilinear(uint32_t *lo, uint32_t *hi, co
 #pragma unroll
     for (int oy = 0; oy < 2; ++oy) {
       const float wyz = w[2][oz] * w[1][oy] * val;
+      const bool pyz = ok[2][oz] && ok[1][oy];
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) {
-        const int sl = base + (oz * A::kSideY + oy) * A::kRow + ox;
-        add_fixed32(lo + sl, hi + sl, __float2int_rn(w[0][ox] * wyz));
+        const int sl = base + (oz * BR + oy) * A::kRow + ox;
+        const int32_t v = __float2int_rn(w[0][ox] * wyz);
+        if (pyz && ok[0][ox]) add_fixed32(lo + sl, hi + sl, v);
       }
     }
 }
 
-// face-normal deposits (particle.cpp:498-524) of a particle in brick-relative cell r3
-// (in [-1, BR - 1] x [-1, BR - 1] x [-1, BZ - 1]): along d, face r3[d] gets (1 - x_l) R_d
-// and face r3[d] + 1 gets x_l R_d, at the particle's cell across. lo[d]/hi[d]: field d's words.
+// face-normal deposits (particle.cpp:498-524) of a particle in brick-relative cell r3:
+// along d, face r3[d] gets (1 - x_l) R_d and face r3[d] + 1 gets x_l R_d, at the
+// particle's cell across; the faces inside the brick are added. lo[d]/hi[d]: field d's words.
 template <int BR, int BZ>
 __device__ __forceinline__ void deposit_faces(uint32_t *const *lo, uint32_t *const *hi, const int r3[3],
                                               const float o3[3], const float ru[3], const float *scale) {
   using A = Acc<BR, BZ>;
+  const int ext[3] = {BR, BR, BZ};
+  bool in[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) in[d] = (unsigned)r3[d] < (unsigned)ext[d];
+  const bool across[3] = {in[1] && in[2], in[0] && in[2], in[0] && in[1]};
   const int sl0 = A::slot(r3[0], r3[1], r3[2]);
-  constexpr int step[3] = {1, A::kRow, A::kSideY * A::kRow};
+  constexpr int step[3] = {1, A::kRow, BR * A::kRow};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float r = ru[d] * scale[1 + d];
-    add_fixed32(lo[d] + sl0, hi[d] + sl0, __float2int_rn((1.f - o3[d]) * r));
-    add_fixed32(lo[d] + sl0 + step[d], hi[d] + sl0 + step[d], __float2int_rn(o3[d] * r));
+    const int32_t v0 = __float2int_rn((1.f - o3[d]) * r), v1 = __float2int_rn(o3[d] * r);
+    if (across[d] && in[d]) add_fixed32(lo[d] + sl0, hi[d] + sl0, v0);
+    if (across[d] && (unsigned)(r3[d] + 1) < (unsigned)ext[d])
+      add_fixed32(lo[d] + sl0 + step[d], hi[d] + sl0 + step[d], v1);
   }
 }
 
@@ -1009,9 +1018,8 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *scrat
 // source window (the particles whose step-start cell lies within two cells of the
 // brick). Per particle, every value the walk may need is loaded at once; then
 //   DO_INT: the concentration and the face momentum at the *_int position (fields
-//     C, RHS_RU x/y/z) count when its x_int cell lies within one cell of the brick --
-//     the trilinear node in the brick's node range, the cell in [-1, B - 1] for the
-//     faces -- and add every target without a test;
+//     C, RHS_RU x/y/z), when its x_int cell lies within one cell of the brick: the
+//     targets inside the brick;
 //   DO_NEW: RHS_T at the *_new position (RHS_Part_Temp), the same way.
 // Field slots: 0 C, 1-3 RHS_RU x/y/z, 4 (FE) RHS_Part_Temp; scale exponents f.se[0..4].
 // Each brick's exact integer field totals are added to `totals` (five int64 words,
@@ -1122,26 +1130,24 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
       if (DO_INT) {
         const int r3[3] = {rel_local(ci_(ci), bx, G.n[0]), rel_local(cj_(ci), by, G.n[1]),
                            rel_local(ck_(ci), bz, G.n[2])};
-        // only a cell within one of the brick reaches it; then every target lies in the accumulator
+        // only a cell within one of the brick reaches it
         if ((unsigned)(r3[0] + 1) <= (unsigned)(BR + 1) && (unsigned)(r3[1] + 1) <= (unsigned)(BR + 1) &&
             (unsigned)(r3[2] + 1) <= (unsigned)(BZ + 1)) {
           const int node[3] = {r3[0] + (oi[0] >= 0.5f ? 1 : 0), r3[1] + (oi[1] >= 0.5f ? 1 : 0),
                                r3[2] + (oi[2] >= 0.5f ? 1 : 0)};
-          // trilinear targets node - 1 .. node meet the brick iff the node is in its node range
-          if ((unsigned)node[0] <= (unsigned)BR && (unsigned)node[1] <= (unsigned)BR &&
-              (unsigned)node[2] <= (unsigned)BZ)
-            deposit_trilinear<BR, BZ>(lo_f[0], hi_f[0], node, oi, scale[0]);
-          // faces r3 .. r3 + 1 along d, r3 across, meet the brick iff r3 is in [-1, B - 1]
-          if (ru_on && r3[0] < BR && r3[1] < BR && r3[2] < BZ) deposit_faces<BR, BZ>(&lo_f[1], &hi_f[1], r3, oi, ru, scale);
+          deposit_trilinear<BR, BZ>(lo_f[0], hi_f[0], node, oi, scale[0]);
+          if (ru_on) deposit_faces<BR, BZ>(&lo_f[1], &hi_f[1], r3, oi, ru, scale);
         }
       }
       if (DO_NEW) {
         const int r3[3] = {rel_local(ci_(cn), bx, G.n[0]), rel_local(cj_(cn), by, G.n[1]),
                            rel_local(ck_(cn), bz, G.n[2])};
-        const int node[3] = {r3[0] + (on3[0] >= 0.5f ? 1 : 0), r3[1] + (on3[1] >= 0.5f ? 1 : 0),
-                             r3[2] + (on3[2] >= 0.5f ? 1 : 0)};
-        if ((unsigned)node[0] <= (unsigned)BR && (unsigned)node[1] <= (unsigned)BR && (unsigned)node[2] <= (unsigned)BZ)
+        if ((unsigned)(r3[0] + 1) <= (unsigned)(BR + 1) && (unsigned)(r3[1] + 1) <= (unsigned)(BR + 1) &&
+            (unsigned)(r3[2] + 1) <= (unsigned)(BZ + 1)) {
+          const int node[3] = {r3[0] + (on3[0] >= 0.5f ? 1 : 0), r3[1] + (on3[1] >= 0.5f ? 1 : 0),
+                               r3[2] + (on3[2] >= 0.5f ? 1 : 0)};
           deposit_trilinear<BR, BZ>(lo_f[FE], hi_f[FE], node, on3, rt * scale[4]);
+        }
       }
     }
     __syncthreads();
@@ -1431,7 +1437,7 @@ int sort_step(pstep_ctx *h) {
     const int nbk = w.nbd;
     const int wblocks = (int)(((int64_t)nbk * 32 + kThreads - 1) / kThreads);  // one warp per brick
     if (w.br == 16)
-      k_work_count<16, 8><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
+      k_work_count<16, 16><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
     else
       k_work_count<8, 8><<<wblocks, kThreads, 0, h->stream>>>(G, f.cell_start, w, nbk);
     PSTEP_LAUNCHED(h);
@@ -1490,16 +1496,17 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->sidx, cap));
   {  // deposit work list
     Work &w = f->work;
-    // 16 x 16 x 8 where the grid allows (the window of a brick and two cells must not
-    // wrap onto itself), else 8 x 8 x 8
-    const bool big = G.n[0] % 16 == 0 && G.n[0] >= 32 && G.n[1] % 16 == 0 && G.n[1] >= 32 && G.n[2] >= 16;
+    // 16^3 where the grid allows (the window of a brick and two cells must not wrap
+    // onto itself), else 8^3
+    bool big = true;
+    for (int d = 0; d < 3; ++d) big = big && G.n[d] % 16 == 0 && G.n[d] >= 32;
     w.br = big ? 16 : 8;
-    w.bz = 8;
+    w.bz = w.br;
     const int64_t nbk = (int64_t)(G.n[0] / w.br) * (G.n[1] / w.br) * (G.n[2] / w.bz);
     w.nbd = (int)nbk;
     // a split brick's window holds more than kChunkMax particles and the windows
     // hold at most kVisit * cap particles in all
-    const int64_t visit = w.br == 16 ? DepTraits<16, 8>::kVisit : DepTraits<8, 8>::kVisit;
+    const int64_t visit = w.br == 16 ? DepTraits<16, 16>::kVisit : DepTraits<8, 8>::kVisit;
     w.slot_cap = visit * (int64_t)h->cap / kChunkMax + 1;
     w.err = h->err_word;
     const int64_t br3 = (int64_t)w.br * w.br * w.bz;
@@ -1888,7 +1895,7 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   double *C = h->dep[PSTEP_FIELD_C], *X = h->dep[PSTEP_FIELD_RU_X], *Y = h->dep[PSTEP_FIELD_RU_Y],
          *Z = h->dep[PSTEP_FIELD_RU_Z], *E = h->dep[PSTEP_FIELD_PART_TEMP];
   if (f.work.br == 16) {
-    TRY32((dep_run<16, 8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E)));
+    TRY32((dep_run<16, 16>(h, do_int, do_new, SI, SN, C, X, Y, Z, E)));
   } else {
     TRY32((dep_run<8, 8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E)));
   }
