@@ -24,10 +24,15 @@ excluded few sit on cell faces: the reference's face-normal interpolation
 particle within the fp32 resolution of a face (about 1e-7 cells) can take the
 neighbouring cell's transverse velocity -- measured: 17 of 2^27 particles move more
 than 1e-6 cells apart, at most 4e-5 cells, every one a particle that crossed a cell
-face during the step (also with scalar tau_p). The momentum fields carry those
-particles' drag, so they are bounded in the L2 norm (and reported in the max norm);
-their totals, the momentum balance, within 1e-5 of the sum of magnitudes. The
-measured report is printed.
+face during the step (also with scalar tau_p).
+The deposited momentum is the drag RHS_u = (u_gas - u_p) / tau_p, a difference of two
+velocities of size u_rms. The particles start at the gas velocity, so after one step
+the slip is about 1e-3 u_rms, and fp32 velocities (relative resolution 6e-8) carry it
+to about 1e-4; tau_p down to 0.01 puts those particles' drag among the largest deposits.
+Measured: RHS_RU fields within 2.5e-4 in the L2 norm and 1e-2 of the maximum (the face
+cases), their totals -- the momentum balance -- within 5e-7 of the sum of magnitudes.
+The momentum fields are bounded at 1e-3 (L2) and 2e-2 (max) accordingly, their totals
+at 1e-5. The measured report is printed.
 """
 import hashlib
 import json
@@ -45,6 +50,7 @@ SIZED = os.path.join(helpers.GOLDEN, "reference_digests_box256.json")
 FIELD_TOL = 1e-12
 MEAN_RTOL = 1e-12
 REL_TOL = 1e-5
+RU_L2_TOL, RU_MAX_TOL = 1e-3, 2e-2  # momentum fields after one step from zero slip (see above)
 
 
 def digest(a) -> str:
@@ -138,7 +144,9 @@ def test_box512_mixed_fp32_error_against_fp64(built_cuda):
                                "rhs_t_rel_to_max_bulk", "energy_mean_rel")
            if not rep[k] <= REL_TOL}
     bad.update({k: v for k, v in rep["fields"].items() if k in ("C", "RHS_Part_Temp") and not v <= REL_TOL})
-    bad.update({"l2_" + k: v for k, v in rep["fields_l2"].items() if not v <= REL_TOL})
+    bad.update({"l2_" + k: v for k, v in rep["fields_l2"].items()
+                if not v <= (REL_TOL if k in ("C", "RHS_Part_Temp") else RU_L2_TOL)})
+    bad.update({k: v for k, v in rep["fields"].items() if k.startswith("RHS_RU") and not v <= RU_MAX_TOL})
     bad.update({k: v for k, v in rep["momentum_rel_to_abs"].items() if not v <= REL_TOL})
     # the face cases are few and stay small
     assert rep["position_cells_count"] <= rep["bulk_excludes"], rep["position_cells_count"]
