@@ -57,13 +57,13 @@ FP64_ADVANCE_CELL_BYTES = 4 * 8
 FP32_ADVANCE_BYTES = {0: 36 + 80, 1: 100 + 80, 2: 100 + 80, 3: 100 + 80}
 FP32_ADVANCE_CELL_BYTES = 4 * 4
 # with the learned correction the advance also reads and writes the drive state
-# (slip 3 + temperature difference, fp32) and reads the kept network output (bf16 x 4):
-# +40 B per particle and stage.
-FP32MLP_ADVANCE_EXTRA = 40
+# (slip 3 + temperature difference, bf16 x 4) and reads the kept network output (bf16 x 4):
+# +24 B per particle and stage.
+FP32MLP_ADVANCE_EXTRA = 24
 # The network kernel (once per step): x_int cell + offsets + u,v,w (28 B), the drive state
-# (16 B), the network output written (8 B) = 52 B per particle; the velocity field (3 fp32)
+# (8 B), the network output written (8 B) = 44 B per particle; the velocity field (3 fp32)
 # once per launch; the weights (13 KB) once per CTA.
-FP32MLP_NETWORK_BYTES = (52.0, 12.0)
+FP32MLP_NETWORK_BYTES = (44.0, 12.0)
 # Deposits, per particle and per cell of one launch:
 #   FP32 (one fused walk): *_int cell+offsets (16) + RHS_u (12) + *_new cell+offsets (16) + RHS_T (4) = 48 B;
 #        per cell: cell_start (4) + five fp64 fields written (40) = 44 B.

@@ -98,7 +98,8 @@ struct F32Form {
   float *itp;      // per-particle 1/tau_p or nullptr
   float *pp[7];    // per-particle mass ratio, itth, 1/(m Cvp), alpha, body acceleration x y z (or nullptr)
   float *gas[4];   // ug vg wg at x_int and Tg - t_ref at x_new of the last stage (PSTEP_KEEP_GAS)
-  float *drive[4]; // learned correction: the slip (3) and T_new - Tg the last stage's drag and heat transfer used
+  uint2 *drive;    // learned correction: the slip (3) and T_new - Tg the last stage's drag and heat transfer
+                   // used, bf16 x 4 (a lagged estimate: bf16's 3 significant digits serve it)
   uint2 *corr_y;   // learned correction: the network output of the step's stage 0 (bf16 x 4)
   float *rhs_u[3];
   float *uf[3], *tf;  // fp32 ghosted copies of the bound fields
@@ -497,9 +498,9 @@ __device__ __forceinline__ void silu_chunk_to_tile(uint8_t *tile, int r, int c0,
 }
 
 // the drive slip: the previous stage's (at most kDriveCap x the plain one), or the plain slip
-__device__ __forceinline__ void drive_slip(const F32Form &f, int64_t p, const float (&s)[3], float smag, float &sdrv,
+__device__ __forceinline__ void drive_slip(const uint2 dw, const float (&s)[3], float smag, float &sdrv,
                                            float (&dir)[3], float &dmag_used) {
-  const float d0 = f.drive[0][p], d1 = f.drive[1][p], d2 = f.drive[2][p];
+  const float d0 = bf16_lo(dw.x), d1 = bf16_hi(dw.x), d2 = bf16_lo(dw.y);
   const float dmag = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
   if (dmag > 0.f) {
     sdrv = fminf(dmag, kDriveCap * smag);
@@ -573,7 +574,7 @@ __global__ void __launch_bounds__(corr::kThreads, 4) k_corr_net(Geom G, F32Form 
         const float s[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
         const float smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
         float sdrv, dir[3], dmag;
-        drive_slip(f, p, s, smag, sdrv, dir, dmag);
+        drive_slip(f.drive[p], s, smag, sdrv, dir, dmag);
         const float itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
         const float itp = f.itp ? f.itp[p] : c.itp;
         const float alpha = f.pp[PP_ALPHA] ? f.pp[PP_ALPHA][p] : c.alpha;
@@ -681,18 +682,18 @@ __global__ void __launch_bounds__(256, 5) k_advance32_corr(Geom G, F32Form f, C3
       const float s[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
       const float smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
       float sdrv, dir[3], dmag;
-      drive_slip(f, p, s, smag, sdrv, dir, dmag);
+      const uint2 dw = f.drive[p];
+      drive_slip(dw, s, smag, sdrv, dir, dmag);
       const float dp = particle_dp(f, cd, p, a.itth);
       const float prior = prior_of(cd, dp * cd.idx, sdrv * dp * cd.inv_nu);
 #pragma unroll
       for (int d = 0; d < 3; ++d) a.gas[d] -= sdrv * prior * yo[d];
       ty = prior * yo[3];
-      td = f.drive[3][p];
+      td = bf16_hi(dw.y);
     }
-    f.drive[0][p] = a.vin[0] - a.gas[0];
-    f.drive[1][p] = a.vin[1] - a.gas[1];
-    f.drive[2][p] = a.vin[2] - a.gas[2];
-    f.drive[3][p] = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, td, err, mu0, mu1, mu2, mt);
+    const float dv[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
+    const float dt_drive = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, td, err, mu0, mu1, mu2, mt);
+    f.drive[p] = make_uint2(pack_bf16x2(dv[0], dv[1]), pack_bf16x2(dv[2], dt_drive));
   }
   block_max4(f.slots, mu0, mu1, mu2, mt);
 }
@@ -1392,8 +1393,6 @@ int sort_step(pstep_ctx *h) {
       if (f.pp[q]) arrs[na++] = &f.pp[q];
     for (int q = 0; q < 4; ++q)
       if (f.gas[q]) arrs[na++] = &f.gas[q];
-    for (int q = 0; q < 4; ++q)
-      if (f.drive[q]) arrs[na++] = &f.drive[q];
     // Scratch: the *_np1 set's 8 arrays. After the step's last stage the base set
     // holds the new positions and every *_int, *_new and *_np1 query reads the base
     // set, so the stage sets carry nothing across the step boundary.
@@ -1427,7 +1426,17 @@ int sort_step(pstep_ctx *h) {
       }
     }
     // f.corr_y (the network output) is not carried: stage 0 rewrites it for every
-    // particle before stages 1-3 read it
+    // particle before stages 1-3 read it, so it is the drive state's scratch here
+    if (f.drive) {
+      PermBatch<uint2> pb{};
+      pb.src[0] = f.drive;
+      pb.dst[0] = f.corr_y;
+      k_perm_batch<uint2, 1><<<pgrid, 256, 0, h->stream>>>(pb, f.sidx, n);
+      PSTEP_LAUNCHED(h);
+      uint2 *t = f.drive;
+      f.drive = f.corr_y;
+      f.corr_y = t;
+    }
     PSTEP_CUDA(cudaMemsetAsync(&f.bounds[4], 0, sizeof(uint32_t), h->stream));
     k_max_count<<<1024, kThreads, 0, h->stream>>>(f.cell_start, ncell, &f.bounds[4]);
     PSTEP_LAUNCHED(h);
@@ -1547,7 +1556,7 @@ int f32_destroy(pstep_ctx *h) {
   if (f->corr_mem) cudaFree(f->corr_mem);
   for (int q = 0; q < 7; ++q) dfree32(f->pp[q]);
   for (int q = 0; q < 4; ++q) dfree32(f->gas[q]);
-  for (int q = 0; q < 4; ++q) dfree32(f->drive[q]);
+  dfree32(f->drive);
   dfree32(f->corr_y);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx);
@@ -1591,8 +1600,7 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
   const int64_t n = h->np;
   dfree32(f.itp);
   for (int q = 0; q < 7; ++q) dfree32(f.pp[q]);
-  for (int q = 0; q < 4; ++q)
-    if (f.drive[q]) PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
+  if (f.drive) PSTEP_CUDA(cudaMemsetAsync(f.drive, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   if (f.corr_y) PSTEP_CUDA(cudaMemsetAsync(f.corr_y, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   f.sorted = 0;
   if (n == 0) return PSTEP_OK;
@@ -1768,10 +1776,8 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
   cd.dp = (float)cfg.dp;
   cd.idx = (float)G.idx[0];
   h->corr_every_stage = pc->every_stage ? 1 : 0;
-  for (int q = 0; q < 4; ++q) {
-    if (!f.drive[q]) TRY32(dalloc32(h, f.drive[q], (size_t)h->cap));
-    PSTEP_CUDA(cudaMemsetAsync(f.drive[q], 0, sizeof(float) * (size_t)h->cap, h->stream));
-  }
+  if (!f.drive) TRY32(dalloc32(h, f.drive, (size_t)h->cap));
+  PSTEP_CUDA(cudaMemsetAsync(f.drive, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   if (!f.corr_y) TRY32(dalloc32(h, f.corr_y, (size_t)h->cap));
   PSTEP_CUDA(cudaMemsetAsync(f.corr_y, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   h->corr_on = 1;

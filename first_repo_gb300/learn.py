@@ -452,10 +452,13 @@ if __name__ == "__main__":
 
     ap = argparse.ArgumentParser(description="train the learned correction on quiescent-gas runs")
     ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--rounds", type=int, default=2, help="closed-loop data rounds before the final training")
+    ap.add_argument("--emphasis", type=float, default=0.0, help="draw training rows with probability prior**emphasis")
     ap.add_argument("--out", default=MODEL_FILE)
     a = ap.parse_args()
-    r = pipeline(steps=a.steps)
+    r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis)
     meta = {k: r[k] for k in ("plain", "corrected", "slip_reduction", "settle_reduction", "temp_reduction", "samples",
-                              "final_loss", "boxes")}
+                              "final_loss", "boxes", "slip_by_k")}
+    meta["settings"] = {"steps": a.steps, "rounds": a.rounds, "emphasis": a.emphasis}
     save_model(r["model"], a.out, meta)
     print(json.dumps(meta))
