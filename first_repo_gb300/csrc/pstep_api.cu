@@ -58,7 +58,7 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
 int f32_set_tau(pstep_ctx *h, const double *tau, int on_device);
 int f32_set_props(pstep_ctx *h, const pstep_particle_props *props, int on_device);
 int f32_set_correction(pstep_ctx *h, const pstep_correction *c);
-int f32_bind_fields(pstep_ctx *h);
+int f32_bind_fields(pstep_ctx *h, int which);
 int f32_prime(pstep_ctx *h);
 int f32_stage(pstep_ctx *h, int k, double pre, double post);
 int f32_end_stage(pstep_ctx *h);
@@ -428,7 +428,7 @@ int pstep_bind_velocity(pstep_handle h, const double *ux, const double *uy, cons
   TRY(copy_field_in(h, uy, on_device, h->own_u[1], h->uy));
   TRY(copy_field_in(h, uz, on_device, h->own_u[2], h->uz));
   h->fields_u++;
-  if (is_f32(h)) TRY(f32_bind_fields(h));
+  if (is_f32(h)) TRY(f32_bind_fields(h, 1));
   return PSTEP_OK;
 }
 
@@ -436,7 +436,7 @@ int pstep_bind_temperature(pstep_handle h, const double *t, int on_device) {
   if (!h) return PSTEP_ERR_ARG;
   TRY(copy_field_in(h, t, on_device, h->own_t, h->tf));
   h->fields_t++;
-  if (is_f32(h)) TRY(f32_bind_fields(h));
+  if (is_f32(h)) TRY(f32_bind_fields(h, 2));
   return PSTEP_OK;
 }
 

@@ -1784,7 +1784,8 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
   return PSTEP_OK;
 }
 
-int f32_bind_fields(pstep_ctx *h) {
+// fp32 copies of the fields just bound: which = 1 the velocity (3 fields), 2 the temperature
+int f32_bind_fields(pstep_ctx *h, int which) {
   F32Form &f = *h->f32;
   const int64_t gs = h->geom.gsize;
   if (h->tf && !f.tref_set) {
@@ -1797,7 +1798,7 @@ int f32_bind_fields(pstep_ctx *h) {
   const double *src[4] = {h->ux, h->uy, h->uz, h->tf};
   float *dst[4] = {f.uf[0], f.uf[1], f.uf[2], f.tf};
   for (int q = 0; q < 4; ++q) {
-    if (!src[q]) continue;
+    if (!src[q] || !(which & (q < 3 ? 1 : 2))) continue;
     k_to_f32<<<nb(gs), kThreads, 0, h->stream>>>(src[q], gs, q == 3 ? f.tref : 0.0, dst[q]);
     PSTEP_LAUNCHED(h);
   }
