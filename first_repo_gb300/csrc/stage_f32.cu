@@ -109,7 +109,8 @@ struct F32Form {
   uint32_t *bounds;   // [0..2] max |RHS_u| per component (float bits), [3] max |RHS_T|, [4] max per-cell count
   uint32_t *slots;    // kBoundSlots x 4 partial maxima (spread so blocks do not contend on one word)
   int32_t *se;        // fixed-point scale exponents per field
-  unsigned long long *totals;  // exact integer totals of the five fields of the last deposit
+  unsigned long long *totals;  // exact integer sums, maxima, minima of the five fields (last deposit)
+  double *fstat;               // per field: max, min, interior sum as fp64 (k_totals)
   Work work;
   int launch_no;      // deposit launches since the last work-list build (counter index)
   void *corr_mem;     // learned correction: packed weight image + biases (device), or nullptr
@@ -997,23 +998,9 @@ template <int BR, int BZ, int NF> struct DepSmem {
   static constexpr int kRanges = Window<BR, BZ>::kRanges;
   static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR, BZ>::kSlots;
   static constexpr size_t kBytes =
-      2 * kAcc + sizeof(long long) * 32 + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
+      2 * kAcc + sizeof(long long) * 32 * 15 + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
   static_assert(kRanges <= 2 * DepTraits<BR, BZ>::kThreads, "ranges exceed the block scan");
 };
-
-// block sum of one int64 per thread; every thread calls it, thread 0 gets the result
-__device__ __forceinline__ long long block_sum_i64(long long v, long long *scratch) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
-  __syncthreads();  // the scratch may still be read by a previous call
-  if (lane == 0) scratch[wid] = v;
-  __syncthreads();
-  long long s = 0;
-  if (threadIdx.x == 0)
-    for (int q = 0; q < nw; ++q) s += scratch[q];  // integer sums: exact in any order
-  return s;
-}
 
 // Deposit into bricks of BR x BR x BZ interior cells, one walk over each brick's
 // source window (the particles whose step-start cell lies within two cells of the
@@ -1023,9 +1010,10 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *scrat
 //     targets inside the brick;
 //   DO_NEW: RHS_T at the *_new position (RHS_Part_Temp), the same way.
 // Field slots: 0 C, 1-3 RHS_RU x/y/z, 4 (FE) RHS_Part_Temp; scale exponents f.se[0..4].
-// Each brick's exact integer field totals are added to `totals` (five int64 words,
-// zeroed before the launch): the momentum and energy balance sums, exact and
-// independent of the order of the work.
+// The flush gathers each brick's exact integer field totals, maxima and minima into
+// `totals` (15 int64 words: sums, maxima, minima of the five fields; k_dep_stats_init
+// sets them before the launch): the momentum and energy balance sums and the field
+// statistics, exact and independent of the order of the work.
 template <bool DO_INT, bool DO_NEW, int BR, int BZ>
 __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
     k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w, int twc, double *__restrict__ outC,
@@ -1039,8 +1027,8 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
   extern __shared__ __align__(16) uint8_t dsm[];
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(dsm);
   uint32_t *acc_hi = acc_lo + NF * SLOTS;
-  long long *red = reinterpret_cast<long long *>(acc_hi + NF * SLOTS);  // 32 (8-byte aligned)
-  int32_t *pre = reinterpret_cast<int32_t *>(red + 32);                 // NR + 1
+  long long *red = reinterpret_cast<long long *>(acc_hi + NF * SLOTS);  // 32 x 15 (8-byte aligned)
+  int32_t *pre = reinterpret_cast<int32_t *>(red + 32 * 15);            // NR + 1
   int32_t *beg = pre + NR + 1;                                          // NR
   int32_t *misc = beg + NR;                                             // 32 warp sums, item, last
   uint32_t *lo_f[5], *hi_f[5];
@@ -1169,7 +1157,9 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
       if (!last) continue;
       __threadfence();
     }
-    long long tot[5] = {0, 0, 0, 0, 0};
+    long long tot[5] = {0, 0, 0, 0, 0}, vmax[5], vmin[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) { vmax[q] = LLONG_MIN; vmin[q] = LLONG_MAX; }
     for (int s = threadIdx.x; s < NB; s += blockDim.x) {
       const int lx = s % BR, ly = (s / BR) % BR, lz = s / (BR * BR);
       const long long g = glin3(G, bx + lx + 1, by + ly + 1, bz + lz + 1);
@@ -1187,29 +1177,79 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
         }
         const bool zero_ru = fld >= 1 && fld <= 3 && !twc;  // RHS_RU = 0 without TWC (grid.cpp:671)
         double *out = fld == 0 ? outC : (fld == 1 ? outX : (fld == 2 ? outY : (fld == 3 ? outZ : outE)));
-        out[g] = zero_ru ? 0.0 : fixed_to_f64(v, se[fld]);
-        tot[fld] += zero_ru ? 0 : v;
+        if (zero_ru) v = 0;
+        out[g] = fixed_to_f64(v, se[fld]);
+        tot[fld] += v;
+        vmax[fld] = max(vmax[fld], v);
+        vmin[fld] = min(vmin[fld], v);
       }
     }
+    // the brick's exact field totals, maxima and minima (integer order is the fp64
+    // order at one scale) into the launch's statistics: sums, then maxima, then minima
 #pragma unroll
-    for (int fld = 0; fld < 5; ++fld) {
-      if (fld < 4 ? !DO_INT : !DO_NEW) continue;
-      const long long sum = block_sum_i64(tot[fld], red);
-      if (threadIdx.x == 0 && sum) atomicAdd(&totals[fld], (unsigned long long)sum);
+    for (int q = 0; q < 5; ++q) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        tot[q] += __shfl_xor_sync(0xffffffffu, tot[q], o);
+        vmax[q] = max(vmax[q], __shfl_xor_sync(0xffffffffu, vmax[q], o));
+        vmin[q] = min(vmin[q], __shfl_xor_sync(0xffffffffu, vmin[q], o));
+      }
+    }
+    {
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+          red[wid * 15 + q] = tot[q];
+          red[wid * 15 + 5 + q] = vmax[q];
+          red[wid * 15 + 10 + q] = vmin[q];
+        }
+      }
+      __syncthreads();
+      const int q = threadIdx.x;
+      if (q < 15 && (q % 5 < 4 ? DO_INT : DO_NEW)) {
+        long long r = red[q];
+        for (int w2 = 1; w2 < nw; ++w2) {
+          const long long x = red[w2 * 15 + q];
+          r = q < 5 ? r + x : (q < 10 ? max(r, x) : min(r, x));
+        }
+        if (q < 5) {
+          if (r) atomicAdd(&totals[q], (unsigned long long)r);
+        } else if (q < 10) {
+          atomicMax(reinterpret_cast<long long *>(&totals[q]), r);
+        } else {
+          atomicMin(reinterpret_cast<long long *>(&totals[q]), r);
+        }
+      }
     }
     if (tile && threadIdx.x == 0) w.done[slot_idx] = 0;
     __syncthreads();
   }
 }
 
-// the balance sums of the last deposit: the exact integer field totals as fp64
-// (correctly rounded), momentum components summed and the energy as the interior mean
+// statistics words of the fields a deposit launch writes: sums 0, maxima and minima at
+// the ends of the int64 range
+__global__ void k_dep_stats_init(unsigned long long *__restrict__ totals, int do_int, int do_new) {
+  const int q = threadIdx.x;
+  if (q >= 15 || !(q % 5 < 4 ? do_int : do_new)) return;
+  totals[q] = q < 5 ? 0ull : (q < 10 ? (unsigned long long)LLONG_MIN : (unsigned long long)LLONG_MAX);
+}
+
+// The balance sums and field statistics of the last deposit, from the exact integer
+// words as fp64 (correctly rounded): the momentum components' sums, the interior mean
+// of RHS_Part_Temp (grid.cpp:541), and per field max, min and interior sum
+// (fstat[3 q .. 3 q + 2]) for the fields this launch wrote.
 __global__ void k_totals(F32Form f, const unsigned long long *__restrict__ totals, int do_int, int do_new,
-                         double inv_cells, double *__restrict__ mom, double *__restrict__ emean) {
-  if (threadIdx.x != 0) return;
-  if (do_int)
-    for (int d = 0; d < 3; ++d) mom[d] = fixed_to_f64((long long)totals[1 + d], f.se[1 + d]);
-  if (do_new) *emean = fixed_to_f64((long long)totals[4], f.se[4]) * inv_cells;
+                         double inv_cells, double *__restrict__ mom, double *__restrict__ emean,
+                         double *__restrict__ fstat) {
+  const int q = threadIdx.x;
+  if (q >= 5 || !(q < 4 ? do_int : do_new)) return;
+  const int se = f.se[q];
+  fstat[3 * q + 0] = fixed_to_f64((long long)totals[5 + q], se);
+  fstat[3 * q + 1] = fixed_to_f64((long long)totals[10 + q], se);
+  fstat[3 * q + 2] = fixed_to_f64((long long)totals[q], se);
+  if (q >= 1 && q <= 3) mom[q - 1] = fstat[3 * q + 2];
+  if (q == 4) *emean = fstat[3 * q + 2] * inv_cells;
 }
 
 __global__ void k_to_f32(const double *__restrict__ src, int64_t n, double shift, float *__restrict__ dst) {
@@ -1538,7 +1578,9 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->slots, kBoundSlots * 4));
   PSTEP_CUDA(cudaMemsetAsync(f->slots, 0, kBoundSlots * 4 * sizeof(uint32_t), h->stream));
   TRY32(dalloc32(h, f->se, 8));
-  TRY32(dalloc32(h, f->totals, 8));
+  TRY32(dalloc32(h, f->totals, 16));
+  TRY32(dalloc32(h, f->fstat, 16));
+  PSTEP_CUDA(cudaMemsetAsync(f->fstat, 0, 16 * sizeof(double), h->stream));
   TRY32(dalloc32(h, h->s.flag, cap));
   PSTEP_CUDA(cudaMemsetAsync(f->bounds, 0, 8 * sizeof(uint32_t), h->stream));
   return PSTEP_OK;
@@ -1560,7 +1602,7 @@ int f32_destroy(pstep_ctx *h) {
   dfree32(f->corr_y);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx);
-  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots); dfree32(f->totals);
+  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots); dfree32(f->totals); dfree32(f->fstat);
   {
     Work &w = f->work;
     dfree32(w.items); dfree32(w.nchunk); dfree32(w.slot); dfree32(w.cnt_a); dfree32(w.cnt_b); dfree32(w.cnt_s);
@@ -1898,7 +1940,8 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   k_scales<<<1, 32, 0, h->stream>>>(f);  // fold this advance's maxima into the fixed-point scales
   PSTEP_LAUNCHED(h);
   PSTEP_CUDA(cudaMemsetAsync(f.work.next, 0, sizeof(int32_t), h->stream));
-  PSTEP_CUDA(cudaMemsetAsync(f.totals, 0, 5 * sizeof(unsigned long long), h->stream));
+  k_dep_stats_init<<<1, 32, 0, h->stream>>>(f.totals, do_int ? 1 : 0, do_new ? 1 : 0);
+  PSTEP_LAUNCHED(h);
   double *C = h->dep[PSTEP_FIELD_C], *X = h->dep[PSTEP_FIELD_RU_X], *Y = h->dep[PSTEP_FIELD_RU_Y],
          *Z = h->dep[PSTEP_FIELD_RU_Z], *E = h->dep[PSTEP_FIELD_PART_TEMP];
   if (f.work.br == 16) {
@@ -1919,11 +1962,15 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   // the interior mean of RHS_Part_Temp (grid.cpp:541)
   const Geom &G = h->geom;
   k_totals<<<1, 32, 0, h->stream>>>(f, f.totals, do_int ? 1 : 0, do_new ? 1 : 0,
-                                    1.0 / ((double)G.n[0] * G.n[1] * G.n[2]), h->mom_dev, h->emean_dev);
+                                    1.0 / ((double)G.n[0] * G.n[1] * G.n[2]), h->mom_dev, h->emean_dev, f.fstat);
   PSTEP_LAUNCHED(h);
   return PSTEP_OK;
 }
 }  // namespace
+
+// device address of a deposited field's max, min and interior sum of the last deposit
+// that wrote it (FP32 form)
+const double *f32_field_stats_dev(pstep_ctx *h, int field) { return h->f32->fstat + 3 * field; }
 
 int f32_end_stage(pstep_ctx *h) {
   F32Form &f = *h->f32;

@@ -194,6 +194,17 @@ int pstep_max(pstep_handle h, int id, double *out) {
 int pstep_field_stats(pstep_handle h, int field, double *max, double *min, double *mean) {
   if (!h || field < 0 || field >= PSTEP_NUM_FIELDS) return PSTEP_ERR_ARG;
   const Geom &G = h->geom;
+  if (h->f32) {
+    // the FP32 form's deposit gathers these in its flush (exact integer max, min, sum)
+    double r[3] = {0, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(r, f32_field_stats_dev(h, field), sizeof r, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail_io(h, PSTEP_ERR_CUDA, std::string("field stats: ") + cudaGetErrorString(e));
+    if (max) *max = r[0];
+    if (min) *min = r[1];
+    if (mean) *mean = r[2] / (double)((long long)G.n[0] * G.n[1] * G.n[2]);
+    return PSTEP_OK;
+  }
   double *part = nullptr;
   int rc = dalloc_tmp(h, part, 3 * kStatBlocks + 3);
   if (rc) return rc;
