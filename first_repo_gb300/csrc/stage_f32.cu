@@ -522,6 +522,24 @@ __device__ __forceinline__ float particle_dp(const F32Form &f, const CorrDev &cd
   return f.pp[PP_ITTH] ? itth * cd.dp_per_itth : cd.dp;
 }
 
+// A particle's network inputs as loaded from memory (x_int cell, offsets and velocity,
+// the drive state), fetched one tile ahead so that their memory round trip overlaps the
+// current tile's tensor-core work
+struct NetRaw {
+  uint32_t cell;
+  float o[3], v[3];
+  uint2 drive;
+};
+template <int K>
+__device__ __forceinline__ void net_raw_load(const F32Form &f, int64_t p, int64_t n, NetRaw &r) {
+  if (p >= n) return;
+  const Set32 &I = (K == 0) ? f.set[SBASE] : f.set[SINT];
+  r.cell = I.cell[p];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) { r.o[d] = I.o[d][p]; r.v[d] = I.v[d][p]; }
+  r.drive = f.drive[p];
+}
+
 // The network of every particle at its x_int position: features from the plain
 // interpolation and the drive state of the previous stage, three tcgen05 layers,
 // the output (bf16 x 4) to f.corr_y (zero outside the training ranges).
@@ -560,8 +578,10 @@ __global__ void __launch_bounds__(corr::kThreads, 4) k_corr_net(Geom G, F32Form 
   bool ok = true;
   bool first = cd.idle_first != 0;
   const int64_t ntiles = (n + corr::kRows - 1) / corr::kRows;
-  for (int64_t tile = (int64_t)blockIdx.x * corr::kGroups + wg; tile < ntiles && ok;
-       tile += (int64_t)gridDim.x * corr::kGroups) {
+  const int64_t tstride = (int64_t)gridDim.x * corr::kGroups;
+  NetRaw raw{};
+  net_raw_load<K>(f, ((int64_t)blockIdx.x * corr::kGroups + wg) * corr::kRows + lt, n, raw);
+  for (int64_t tile = (int64_t)blockIdx.x * corr::kGroups + wg; tile < ntiles && ok; tile += tstride) {
     const int64_t p = tile * corr::kRows + lt;
     const bool live = p < n;
     bool use = false;
@@ -570,12 +590,16 @@ __global__ void __launch_bounds__(corr::kThreads, 4) k_corr_net(Geom G, F32Form 
 #pragma unroll
       for (int j = 0; j < corr::kInP; ++j) x[j] = 0.f;
       if (live) {
-        Adv a;
-        adv_load_gas<K>(G, f, p, a);
-        const float s[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
+        // the plain interpolation at x_int (particle.cpp:340-360) from the prefetched inputs
+        const int ii = ci_(raw.cell) + 1, jj = cj_(raw.cell) + 1, kk = ck_(raw.cell) + 1;
+        const float gas[3] = {
+            raw.o[0] * f.uf[0][glin3(G, ii + 1, jj, kk)] + (1.f - raw.o[0]) * f.uf[0][glin3(G, ii, jj, kk)],
+            raw.o[1] * f.uf[1][glin3(G, ii, jj + 1, kk)] + (1.f - raw.o[1]) * f.uf[1][glin3(G, ii, jj, kk)],
+            raw.o[2] * f.uf[2][glin3(G, ii, jj, kk + 1)] + (1.f - raw.o[2]) * f.uf[2][glin3(G, ii, jj, kk)]};
+        const float s[3] = {raw.v[0] - gas[0], raw.v[1] - gas[1], raw.v[2] - gas[2]};
         const float smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
         float sdrv, dir[3], dmag;
-        drive_slip(f.drive[p], s, smag, sdrv, dir, dmag);
+        drive_slip(raw.drive, s, smag, sdrv, dir, dmag);
         const float itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
         const float itp = f.itp ? f.itp[p] : c.itp;
         const float alpha = f.pp[PP_ALPHA] ? f.pp[PP_ALPHA][p] : c.alpha;
@@ -588,10 +612,10 @@ __global__ void __launch_bounds__(corr::kThreads, 4) k_corr_net(Geom G, F32Form 
               rep <= cd.hi[1] && q >= cd.lo[2] && q <= cd.hi[2] && taup >= cd.lo[3] && taup <= cd.hi[3];
         if (use) {
           const float inv = 1.f / dmag;
-          const float raw[10] = {a.oin[0], a.oin[1], a.oin[2], dir[0] * inv, dir[1] * inv, dir[2] * inv, dpdx,
+          const float fin[10] = {raw.o[0], raw.o[1], raw.o[2], dir[0] * inv, dir[1] * inv, dir[2] * inv, dpdx,
                                  logf(rep), q, logf(taup)};
 #pragma unroll
-          for (int j = 0; j < 10; ++j) x[j] = (raw[j] - cd.shift[j]) * cd.scale[j];
+          for (int j = 0; j < 10; ++j) x[j] = (fin[j] - cd.shift[j]) * cd.scale[j];
         }
       }
 #pragma unroll
@@ -609,6 +633,7 @@ __global__ void __launch_bounds__(corr::kThreads, 4) k_corr_net(Geom G, F32Form 
       mma_bf16(tcol, tile_desc(sX, corr::kInP, 0, 0), tile_desc(sW1, corr::kInP, 0, 0), id64, 0);
       commit(mbar);
     }
+    net_raw_load<K>(f, (tile + tstride) * corr::kRows + lt, n, raw);  // the next tile's inputs, in flight
     // (the timeout test polls the idle barrier here, as a completion that never arrives;
     // the MMA's own completion is then drained below before the tensor memory is freed)
     ok = group_wait(wg, first ? idle : mbar, phase, limit);
