@@ -120,23 +120,27 @@ def test_training_kernels_fit_quiescent_data(built_cuda):
 def test_quiescent_gas_correction(built_cuda):
     """The committed network (trained by `python -m first_repo_gb300.learn`: 8 boxes x 512
     particles x 200 steps, plain and two closed-loop rounds, 20k Adam steps of 8192) on
-    held-out quiescent boxes with isolated particles (32 dx apart), corrected against plain:
+    held-out quiescent boxes with isolated particles (32 dx apart), corrected against plain,
+    with the network once per step and bf16 drive state:
       settling error (final particle velocity against its true terminal velocity)  >= 5x less,
       gas temperature error at the particles (in units of Q tau_T)                 >= 5x less,
-      gas velocity error at the particles (in units of the terminal slip)          >= 2.4x less.
-    The last is limited by particles with a self-disturbance per unit slip K >= 0.8 (large
-    particles in the most viscous boxes), where the self-consistent correction exceeds the
-    drive cap or does not exist (K >= 1)."""
+      gas velocity error at the particles (the self-induced slip error, in units
+      of the terminal slip)                                                         >= 3.3x less.
+    Measured: 3.7x for the last (3.5-5.5x per box); the target is 5x. Binned by K, the
+    disturbance per unit slip, the particles with K >= 0.9 (large particles in the most
+    viscous boxes) gain least: their plain slip, against which the drive is capped (10x),
+    vanishes as K approaches 1. The per-bin report is printed."""
     model = learn.load_model()
     r = learn.evaluate(model)
     summary = {k: r[k] for k in ("plain", "corrected", "slip_reduction", "settle_reduction", "temp_reduction")}
+    print("quiescent-gas correction:", json.dumps(summary), "by K:", json.dumps(r["slip_by_k"]))
     out = os.environ.get("PSTEP_LEARN_REPORT")
     if out:
         with open(out, "w") as f:
-            json.dump(dict(summary, boxes=r["boxes"]), f, indent=1)
+            json.dump(dict(summary, boxes=r["boxes"], slip_by_k=r["slip_by_k"]), f, indent=1)
     assert r["settle_reduction"] >= 5.0, summary
     assert r["temp_reduction"] >= 5.0, summary
-    assert r["slip_reduction"] >= 2.4, summary
+    assert r["slip_reduction"] >= 3.3, summary
 
 
 def test_once_per_step_inference_matches_every_stage(built_cuda):
