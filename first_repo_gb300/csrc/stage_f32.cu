@@ -424,6 +424,7 @@ struct CorrDev {
   uint32_t wait_limit; // polls of each MMA completion wait (the drain before freeing tensor memory
                        // always allows corr::kWaitLimit)
   uint32_t idle_first; // 1: each warpgroup's first completion wait polls the idle barrier (test)
+  float drive_cap;     // the drive slip at most this many times the plain slip
 };
 
 static_assert(sizeof(CorrDev) <= sizeof(((pstep_ctx *)nullptr)->corr_dev), "correction constants");
@@ -498,13 +499,13 @@ __device__ __forceinline__ void silu_chunk_to_tile(uint8_t *tile, int r, int c0,
   }
 }
 
-// the drive slip: the previous stage's (at most kDriveCap x the plain one), or the plain slip
-__device__ __forceinline__ void drive_slip(const uint2 dw, const float (&s)[3], float smag, float &sdrv,
+// the drive slip: the previous stage's (at most `cap` x the plain one), or the plain slip
+__device__ __forceinline__ void drive_slip(const uint2 dw, const float (&s)[3], float smag, float cap, float &sdrv,
                                            float (&dir)[3], float &dmag_used) {
   const float d0 = bf16_lo(dw.x), d1 = bf16_hi(dw.x), d2 = bf16_lo(dw.y);
   const float dmag = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
   if (dmag > 0.f) {
-    sdrv = fminf(dmag, kDriveCap * smag);
+    sdrv = fminf(dmag, cap * smag);
     dir[0] = d0; dir[1] = d1; dir[2] = d2;
     dmag_used = dmag;
   } else {
@@ -599,7 +600,7 @@ __global__ void __launch_bounds__(corr::kThreads, 4) k_corr_net(Geom G, F32Form 
         const float s[3] = {raw.v[0] - gas[0], raw.v[1] - gas[1], raw.v[2] - gas[2]};
         const float smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
         float sdrv, dir[3], dmag;
-        drive_slip(raw.drive, s, smag, sdrv, dir, dmag);
+        drive_slip(raw.drive, s, smag, cd.drive_cap, sdrv, dir, dmag);
         const float itth = f.pp[PP_ITTH] ? f.pp[PP_ITTH][p] : c.itth;
         const float itp = f.itp ? f.itp[p] : c.itp;
         const float alpha = f.pp[PP_ALPHA] ? f.pp[PP_ALPHA][p] : c.alpha;
@@ -709,7 +710,7 @@ __global__ void __launch_bounds__(256, 5) k_advance32_corr(Geom G, F32Form f, C3
       const float smag = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
       float sdrv, dir[3], dmag;
       const uint2 dw = f.drive[p];
-      drive_slip(dw, s, smag, sdrv, dir, dmag);
+      drive_slip(dw, s, smag, cd.drive_cap, sdrv, dir, dmag);
       const float dp = particle_dp(f, cd, p, a.itth);
       const float prior = prior_of(cd, dp * cd.idx, sdrv * dp * cd.inv_nu);
 #pragma unroll
@@ -1843,6 +1844,7 @@ int f32_set_correction(pstep_ctx *h, const pstep_correction *pc) {
   cd.dp = (float)cfg.dp;
   cd.idx = (float)G.idx[0];
   h->corr_every_stage = pc->every_stage ? 1 : 0;
+  cd.drive_cap = pc->drive_cap > 0.f ? pc->drive_cap : kDriveCap;
   if (!f.drive) TRY32(dalloc32(h, f.drive, (size_t)h->cap));
   PSTEP_CUDA(cudaMemsetAsync(f.drive, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   if (!f.corr_y) TRY32(dalloc32(h, f.corr_y, (size_t)h->cap));

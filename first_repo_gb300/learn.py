@@ -368,7 +368,7 @@ def save_model(model: dict, path: str = MODEL_FILE, meta: dict | None = None):
 
 def load_model(path: str = MODEL_FILE) -> dict:
     z = np.load(path)
-    return {k: z[k] for k in ("params", "shift", "scale", "lo", "hi", "prior_re") if k in z}
+    return {k: z[k] for k in ("params", "shift", "scale", "lo", "hi", "prior_re", "drive_cap") if k in z}
 
 
 def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, eval_runs: int | None = None,

@@ -46,7 +46,7 @@ class Props(C.Structure):
 class Correction(C.Structure):
     _fields_ = [("params", C.POINTER(C.c_float)), ("shift", C.c_float * 10), ("scale", C.c_float * 10),
                 ("lo", C.c_float * 4), ("hi", C.c_float * 4), ("prior_re", C.c_float), ("nu_gas", C.c_double),
-                ("every_stage", C.c_int32)]
+                ("every_stage", C.c_int32), ("drive_cap", C.c_float)]
 
 
 class Config(C.Structure):
@@ -248,6 +248,7 @@ class ParticleStep:
         c.prior_re = float(model.get("prior_re", 0.0))
         c.nu_gas = float(nu_gas if nu_gas is not None else model["nu_gas"])
         c.every_stage = 1 if every_stage else 0
+        c.drive_cap = float(model.get("drive_cap", 0.0))
         self._ok(self.L.pstep_set_correction(self.h, C.byref(c)))
 
     def set_wait_limit(self, polls: int = 0, idle_first: bool = False):

@@ -190,6 +190,10 @@ typedef struct pstep_correction {
   int32_t every_stage;       /* 0: the network runs at stage 0 and its output serves the step's
                                 four stages (each with its own drive slip and prior); 1: it runs
                                 at every stage, at that stage's x_int */
+  float drive_cap;           /* the drive slip is at most drive_cap times the plain slip (a bound
+                                on the lagged iteration; output y < 1 converges to a drive of
+                                plain / (1 - y), so the cap admits y up to 1 - 1/drive_cap);
+                                0: 10 */
 } pstep_correction;
 /* NULL switches the correction off */
 int pstep_set_correction(pstep_handle h, const pstep_correction *c);
