@@ -373,7 +373,7 @@ def load_model(path: str = MODEL_FILE) -> dict:
 
 def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, eval_runs: int | None = None,
              steps: int = 20000, batch: int = 8192, lr: float = 1e-3, eval_lattice: int = 32, rounds: int = 2,
-             emphasis: float = 0.0, log=print) -> dict:
+             emphasis: float = 0.0, drive_cap: float = 0.0, log=print) -> dict:
     """Generate the training set, train, and compare plain and corrected steps on held-out boxes.
 
     Data: the plain two-way-coupled runs, then `rounds` times the same boxes run with the
@@ -397,6 +397,8 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
     for rnd in range(rounds):
         net_model, loss1, _ = train(np.concatenate(f_all), np.concatenate(y_all), steps=steps // 2, batch=batch, lr=lr,
                                     seed=seed + 100 * rnd, emphasis=emphasis)
+        if drive_cap > 0:
+            net_model["drive_cap"] = np.float32(drive_cap)
         log(f"round {rnd} network: loss {loss1[-100:].mean():.4e}")
         for r, run in enumerate(runs):
             f, y, _ = raw_features(spec, run_box(spec, run, net_model))
@@ -406,6 +408,8 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
     f = np.concatenate(f_all)
     y = np.concatenate(y_all)
     model, loss, net = train(f, y, steps=steps, batch=batch, lr=lr, seed=seed + 7, emphasis=emphasis)
+    if drive_cap > 0:
+        model["drive_cap"] = np.float32(drive_cap)
     log(f"trained: loss {loss[:10].mean():.4e} -> {loss[-100:].mean():.4e}")
     out = evaluate(model, spec, eval_seed, eval_lattice, eval_runs, log)
     out["samples"] = int(len(f))
@@ -454,11 +458,12 @@ if __name__ == "__main__":
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--rounds", type=int, default=2, help="closed-loop data rounds before the final training")
     ap.add_argument("--emphasis", type=float, default=0.0, help="draw training rows with probability prior**emphasis")
+    ap.add_argument("--drive-cap", type=float, default=0.0, help="drive slip cap in units of the plain slip (0: 10)")
     ap.add_argument("--out", default=MODEL_FILE)
     a = ap.parse_args()
-    r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis)
+    r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis, drive_cap=a.drive_cap)
     meta = {k: r[k] for k in ("plain", "corrected", "slip_reduction", "settle_reduction", "temp_reduction", "samples",
                               "final_loss", "boxes", "slip_by_k")}
-    meta["settings"] = {"steps": a.steps, "rounds": a.rounds, "emphasis": a.emphasis}
+    meta["settings"] = {"steps": a.steps, "rounds": a.rounds, "emphasis": a.emphasis, "drive_cap": a.drive_cap}
     save_model(r["model"], a.out, meta)
     print(json.dumps(meta))
