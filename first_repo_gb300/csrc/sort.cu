@@ -84,27 +84,51 @@ __global__ void k_scan_blocks(int32_t *__restrict__ sums, int64_t nb) {
 // phase 3: per-tile exclusive scan in blocked order; writes out[0..n] (out[n] = total)
 __global__ void k_scan_apply(const int32_t *__restrict__ in, int64_t n, const int32_t *__restrict__ block_off,
                              int32_t *__restrict__ out, int32_t *__restrict__ out2) {
+  static_assert(kScanItems % 4 == 0, "whole 16-byte vectors per thread");
   __shared__ int32_t sm[kThreads / 32];
   int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  // whole tiles move as 16-byte vectors (the arrays are 16-byte aligned and base is a
+  // multiple of 4 elements); the ragged last tile element by element
+  const bool whole = base + kScanItems <= n && (((uintptr_t)in | (uintptr_t)out | (uintptr_t)out2) & 15) == 0;
   int32_t v[kScanItems];
   int32_t s = 0;
+  if (whole) {
 #pragma unroll
-  for (int q = 0; q < kScanItems; ++q) {
-    int64_t i = base + q;
-    v[q] = i < n ? in[i] : 0;
-    s += v[q];
+    for (int q = 0; q < kScanItems; q += 4) {
+      const int4 a = *reinterpret_cast<const int4 *>(in + base + q);
+      v[q] = a.x; v[q + 1] = a.y; v[q + 2] = a.z; v[q + 3] = a.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) v[q] = base + q < n ? in[base + q] : 0;
   }
+#pragma unroll
+  for (int q = 0; q < kScanItems; ++q) s += v[q];
   int32_t total;
   int32_t e = block_excl_scan(s, sm, total) + block_off[blockIdx.x];
+  if (whole) {
 #pragma unroll
-  for (int q = 0; q < kScanItems; ++q) {
-    int64_t i = base + q;
-    if (i < n) {
-      out[i] = e;
-      if (out2) out2[i] = e;
+    for (int q = 0; q < kScanItems; q += 4) {
+      int4 o;
+      o.x = e; e += v[q];
+      o.y = e; e += v[q + 1];
+      o.z = e; e += v[q + 2];
+      o.w = e; e += v[q + 3];
+      *reinterpret_cast<int4 *>(out + base + q) = o;
+      if (out2) *reinterpret_cast<int4 *>(out2 + base + q) = o;
     }
-    e += v[q];
-    if (i == n - 1) out[n] = e;
+    if (base + kScanItems == n) out[n] = e;
+  } else {
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+      int64_t i = base + q;
+      if (i < n) {
+        out[i] = e;
+        if (out2) out2[i] = e;
+      }
+      e += v[q];
+      if (i == n - 1) out[n] = e;
+    }
   }
 }
 

@@ -1018,15 +1018,43 @@ __device__ __forceinline__ void block_exclusive_scan2(int32_t *a, int n, int32_t
 }
 
 // Shared memory of the deposit CTA for bricks BR x BR x BZ: the accumulators of the NF
-// fields (two words per slot; a multiple of 8 bytes), block-reduction scratch (32
-// int64), the window's row-segment prefix and starts, misc words.
+// fields (two words per slot; a multiple of 8 bytes), each warp's running field sums,
+// maxima and minima (32 x 5 x 3 int64), the window's row-segment prefix and starts,
+// misc words. Whatever shared memory the CTA takes is the L1's loss: at 1024 threads
+// per SM the deposit's loads want every KB of L1 (measured: 40 KB more shared memory,
+// 24% slower), so nothing per thread lives here.
 template <int BR, int BZ, int NF> struct DepSmem {
   static constexpr int kRanges = Window<BR, BZ>::kRanges;
   static constexpr size_t kAcc = sizeof(uint32_t) * NF * Acc<BR, BZ>::kSlots;
-  static constexpr size_t kBytes =
-      2 * kAcc + sizeof(long long) * 32 * 15 + sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
+  static constexpr size_t kBytes = 2 * kAcc + sizeof(long long) * 32 * 5 * 3 +
+                                   sizeof(int32_t) * (2 * kRanges + 1) + sizeof(int32_t) * 40;
   static_assert(kRanges <= 2 * DepTraits<BR, BZ>::kThreads, "ranges exceed the block scan");
+  static_assert(kBytes <= 227 * 1024, "deposit shared memory exceeds the per-block limit");
 };
+
+// warp sum, maximum and minimum of an int64 with 32-bit warp reductions. The sum: three
+// pieces of the two's-complement value (bits 0-20 and 21-41 unsigned, 42-63 signed),
+// whose 32-lane sums cannot overflow, recombined exactly. The maximum and minimum: the
+// high words (signed), then the low words (unsigned) of the lanes holding that high word.
+__device__ __forceinline__ long long warp_sum_i64(long long v) {
+  const unsigned lo = (unsigned)(v & 0x1fffffll), mid = (unsigned)((v >> 21) & 0x1fffffll);
+  const int hi = (int)(v >> 42);
+  const unsigned slo = __reduce_add_sync(0xffffffffu, lo), smid = __reduce_add_sync(0xffffffffu, mid);
+  const int shi = __reduce_add_sync(0xffffffffu, hi);
+  return (long long)shi * (1ll << 42) + (long long)smid * (1ll << 21) + (long long)slo;
+}
+__device__ __forceinline__ long long warp_max_i64(long long v) {
+  const int hi = (int)(v >> 32);
+  const int mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? (unsigned)v : 0u);
+  return (long long)(((unsigned long long)(unsigned)mh << 32) | ml);
+}
+__device__ __forceinline__ long long warp_min_i64(long long v) {
+  const int hi = (int)(v >> 32);
+  const int mh = __reduce_min_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_min_sync(0xffffffffu, hi == mh ? (unsigned)v : 0xffffffffu);
+  return (long long)(((unsigned long long)(unsigned)mh << 32) | ml);
+}
 
 // Deposit into bricks of BR x BR x BZ interior cells, one walk over each brick's
 // source window (the particles whose step-start cell lies within two cells of the
@@ -1036,10 +1064,12 @@ template <int BR, int BZ, int NF> struct DepSmem {
 //     targets inside the brick;
 //   DO_NEW: RHS_T at the *_new position (RHS_Part_Temp), the same way.
 // Field slots: 0 C, 1-3 RHS_RU x/y/z, 4 (FE) RHS_Part_Temp; scale exponents f.se[0..4].
-// The flush gathers each brick's exact integer field totals, maxima and minima into
-// `totals` (15 int64 words: sums, maxima, minima of the five fields; k_dep_stats_init
-// sets them before the launch): the momentum and energy balance sums and the field
-// statistics, exact and independent of the order of the work.
+// The flush also gathers the launch's exact field statistics into `totals` (15 int64
+// words: sums, maxima, minima of the five fields; k_dep_stats_init sets them before the
+// launch): each warp folds the sums, maxima and minima of the cells it flushes into its
+// own running words (warp reductions, no block barrier), and at the end of the launch
+// the block reduces them once. They are the momentum and energy balance sums and the
+// field statistics, exact and independent of the order of the work.
 template <bool DO_INT, bool DO_NEW, int BR, int BZ>
 __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
     k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w, int twc, double *__restrict__ outC,
@@ -1053,8 +1083,11 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
   extern __shared__ __align__(16) uint8_t dsm[];
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(dsm);
   uint32_t *acc_hi = acc_lo + NF * SLOTS;
-  long long *red = reinterpret_cast<long long *>(acc_hi + NF * SLOTS);  // 32 x 15 (8-byte aligned)
-  int32_t *pre = reinterpret_cast<int32_t *>(red + 32 * 15);            // NR + 1
+  constexpr int T = DepTraits<BR, BZ>::kThreads;
+  long long *wsum = reinterpret_cast<long long *>(acc_hi + NF * SLOTS);  // 32 x 5 (8-byte aligned)
+  long long *wmax = wsum + 32 * 5;                                       // 32 x 5
+  long long *wmin = wmax + 32 * 5;                                       // 32 x 5
+  int32_t *pre = reinterpret_cast<int32_t *>(wmin + 32 * 5);             // NR + 1
   int32_t *beg = pre + NR + 1;                                          // NR
   int32_t *misc = beg + NR;                                             // 32 warp sums, item, last
   uint32_t *lo_f[5], *hi_f[5];
@@ -1071,6 +1104,11 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
 #pragma unroll
   for (int q = 0; q < 5; ++q) se[q] = f.se[q];
   const bool ru_on = DO_INT && twc;
+  if ((threadIdx.x & 31) < 5) {  // this warp's own words
+    wsum[(threadIdx.x >> 5) * 5 + (threadIdx.x & 31)] = 0;
+    wmax[(threadIdx.x >> 5) * 5 + (threadIdx.x & 31)] = LLONG_MIN;
+    wmin[(threadIdx.x >> 5) * 5 + (threadIdx.x & 31)] = LLONG_MAX;
+  }
   while (true) {
     if (threadIdx.x == 0) misc[32] = atomicAdd(&w.next[0], 1);
     __syncthreads();
@@ -1210,46 +1248,39 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
         vmin[fld] = min(vmin[fld], v);
       }
     }
-    // the brick's exact field totals, maxima and minima (integer order is the fp64
-    // order at one scale) into the launch's statistics: sums, then maxima, then minima
-#pragma unroll
-    for (int q = 0; q < 5; ++q) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        tot[q] += __shfl_xor_sync(0xffffffffu, tot[q], o);
-        vmax[q] = max(vmax[q], __shfl_xor_sync(0xffffffffu, vmax[q], o));
-        vmin[q] = min(vmin[q], __shfl_xor_sync(0xffffffffu, vmin[q], o));
-      }
-    }
     {
-      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
-      if (lane == 0) {
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
-          red[wid * 15 + q] = tot[q];
-          red[wid * 15 + 5 + q] = vmax[q];
-          red[wid * 15 + 10 + q] = vmin[q];
-        }
-      }
-      __syncthreads();
-      const int q = threadIdx.x;
-      if (q < 15 && (q % 5 < 4 ? DO_INT : DO_NEW)) {
-        long long r = red[q];
-        for (int w2 = 1; w2 < nw; ++w2) {
-          const long long x = red[w2 * 15 + q];
-          r = q < 5 ? r + x : (q < 10 ? max(r, x) : min(r, x));
-        }
-        if (q < 5) {
-          if (r) atomicAdd(&totals[q], (unsigned long long)r);
-        } else if (q < 10) {
-          atomicMax(reinterpret_cast<long long *>(&totals[q]), r);
-        } else {
-          atomicMin(reinterpret_cast<long long *>(&totals[q]), r);
+      for (int fld = 0; fld < 5; ++fld) {
+        if (fld < 4 ? !DO_INT : !DO_NEW) continue;
+        const long long sm = warp_sum_i64(tot[fld]);
+        const long long mx = warp_max_i64(vmax[fld]), mn = warp_min_i64(vmin[fld]);
+        if (lane == 0) {
+          wsum[wid * 5 + fld] += sm;
+          wmax[wid * 5 + fld] = max(wmax[wid * 5 + fld], mx);
+          wmin[wid * 5 + fld] = min(wmin[wid * 5 + fld], mn);
         }
       }
     }
     if (tile && threadIdx.x == 0) w.done[slot_idx] = 0;
     __syncthreads();
+  }
+  // the launch's exact field statistics (integer order is the fp64 order at one scale):
+  // one block reduction of the warps' running words, three atomics per field and block
+  {
+    const int q = threadIdx.x;
+    if (q < NF) {
+      const int fld = DO_INT ? q : 4;
+      long long r = 0, mx = LLONG_MIN, mn = LLONG_MAX;
+      for (int w2 = 0; w2 < T / 32; ++w2) {
+        r += wsum[w2 * 5 + fld];
+        mx = max(mx, wmax[w2 * 5 + fld]);
+        mn = min(mn, wmin[w2 * 5 + fld]);
+      }
+      if (r) atomicAdd(&totals[fld], (unsigned long long)r);
+      atomicMax(reinterpret_cast<long long *>(&totals[5 + fld]), mx);
+      atomicMin(reinterpret_cast<long long *>(&totals[10 + fld]), mn);
+    }
   }
 }
 

@@ -272,12 +272,45 @@ def prior(f: np.ndarray) -> np.ndarray:
     return dpdx / (1.0 + np.exp(f[:, 7]) / dpdx / PRIOR_RE)
 
 
+_PERMS = np.array([(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)])
+
+
+def symmetry_images(f: np.ndarray, y: np.ndarray, copies: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """The samples and `copies` images of each under random elements of the cube's symmetry
+    group (48: axis permutations times reflections about the cell centre). The quiescent box
+    is invariant under them -- cubic cells, the staggered grid's faces and nodes map to
+    faces and nodes, the schemes are centred, the gas is at rest -- so a particle at in-cell
+    offset o moving along d has the image's disturbance: new axis a takes old axis P[a],
+    offsets o'[a] = o[P[a]] (1 - o[P[a]] when reflected), the slip direction and the
+    velocity targets as vectors (sign S[a]), the temperature target and the scalar
+    features unchanged."""
+    if copies <= 0:
+        return f, y
+    rng = np.random.default_rng(seed)
+    fs, ys = [f], [y]
+    rows = np.arange(len(f))[:, None]
+    for _ in range(copies):
+        P = _PERMS[rng.integers(0, 6, len(f))]
+        S = 1.0 - 2.0 * ((rng.integers(0, 8, len(f))[:, None] >> np.arange(3)) & 1)
+        g = f.copy()
+        o = f[:, :3][rows, P]
+        g[:, :3] = np.where(S < 0, 1.0 - o, o)
+        g[:, 3:6] = f[:, 3:6][rows, P] * S
+        z = y.copy()
+        z[:, :3] = y[:, :3][rows, P] * S
+        fs.append(g)
+        ys.append(z)
+    return np.concatenate(fs), np.concatenate(ys)
+
+
 def train(f: np.ndarray, y: np.ndarray, steps: int = 20000, batch: int = 8192, lr: float = 1e-3, seed: int = 0,
-          emphasis: float = 0.0):
+          emphasis: float = 0.0, symmetries: int = 0):
     """Adam on the mean squared error of the targets in units of the prior. emphasis > 0 draws
     the training rows with probability proportional to prior ** emphasis (seeded), so that the
     particles with the largest disturbance per unit slip -- whose error dominates the
-    self-induced slip error -- weigh more."""
+    self-induced slip error -- weigh more. symmetries > 0 adds that many images of every
+    sample under the box's symmetries (symmetry_images)."""
+    f, y = symmetry_images(f, y, symmetries, seed + 29)
     shift, scale, lo, hi = normaliser(f)
     pr = prior(f)
     if emphasis > 0:
@@ -373,7 +406,7 @@ def load_model(path: str = MODEL_FILE) -> dict:
 
 def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, eval_runs: int | None = None,
              steps: int = 20000, batch: int = 8192, lr: float = 1e-3, eval_lattice: int = 32, rounds: int = 2,
-             emphasis: float = 0.0, drive_cap: float = 0.0, log=print) -> dict:
+             emphasis: float = 0.0, drive_cap: float = 0.0, symmetries: int = 0, log=print) -> dict:
     """Generate the training set, train, and compare plain and corrected steps on held-out boxes.
 
     Data: the plain two-way-coupled runs, then `rounds` times the same boxes run with the
@@ -396,7 +429,7 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
     net_model = None
     for rnd in range(rounds):
         net_model, loss1, _ = train(np.concatenate(f_all), np.concatenate(y_all), steps=steps // 2, batch=batch, lr=lr,
-                                    seed=seed + 100 * rnd, emphasis=emphasis)
+                                    seed=seed + 100 * rnd, emphasis=emphasis, symmetries=symmetries)
         if drive_cap > 0:
             net_model["drive_cap"] = np.float32(drive_cap)
         log(f"round {rnd} network: loss {loss1[-100:].mean():.4e}")
@@ -407,7 +440,8 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
         log(f"round {rnd}: closed-loop samples from {len(runs)} boxes")
     f = np.concatenate(f_all)
     y = np.concatenate(y_all)
-    model, loss, net = train(f, y, steps=steps, batch=batch, lr=lr, seed=seed + 7, emphasis=emphasis)
+    model, loss, net = train(f, y, steps=steps, batch=batch, lr=lr, seed=seed + 7, emphasis=emphasis,
+                             symmetries=symmetries)
     if drive_cap > 0:
         model["drive_cap"] = np.float32(drive_cap)
     log(f"trained: loss {loss[:10].mean():.4e} -> {loss[-100:].mean():.4e}")
@@ -459,11 +493,13 @@ if __name__ == "__main__":
     ap.add_argument("--rounds", type=int, default=2, help="closed-loop data rounds before the final training")
     ap.add_argument("--emphasis", type=float, default=0.0, help="draw training rows with probability prior**emphasis")
     ap.add_argument("--drive-cap", type=float, default=0.0, help="drive slip cap in units of the plain slip (0: 10)")
+    ap.add_argument("--symmetries", type=int, default=0, help="images of each sample under the box's symmetries")
     ap.add_argument("--out", default=MODEL_FILE)
     a = ap.parse_args()
-    r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis, drive_cap=a.drive_cap)
+    r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis, drive_cap=a.drive_cap, symmetries=a.symmetries)
     meta = {k: r[k] for k in ("plain", "corrected", "slip_reduction", "settle_reduction", "temp_reduction", "samples",
                               "final_loss", "boxes", "slip_by_k")}
-    meta["settings"] = {"steps": a.steps, "rounds": a.rounds, "emphasis": a.emphasis, "drive_cap": a.drive_cap}
+    meta["settings"] = {"steps": a.steps, "rounds": a.rounds, "emphasis": a.emphasis, "drive_cap": a.drive_cap,
+                        "symmetries": a.symmetries}
     save_model(r["model"], a.out, meta)
     print(json.dumps(meta))

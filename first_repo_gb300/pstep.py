@@ -251,6 +251,11 @@ class ParticleStep:
         c.drive_cap = float(model.get("drive_cap", 0.0))
         self._ok(self.L.pstep_set_correction(self.h, C.byref(c)))
 
+    def set_stream(self, stream: int):
+        """the CUDA stream (cudaStream_t as an int; 0 = the default stream) this handle
+        enqueues its work on (pstep_set_stream)"""
+        self._ok(self.L.pstep_set_stream(self.h, C.c_void_p(int(stream))))
+
     def set_wait_limit(self, polls: int = 0, idle_first: bool = False):
         """bound of the fused inference's tensor-core completion waits (0: default); idle_first
         makes each warpgroup's first wait poll a barrier that nothing signals (timeout test)"""

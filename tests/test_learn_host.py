@@ -103,3 +103,35 @@ def test_slip_error_binned_by_k():
     for b in bins:
         assert abs(b["reduction"] - 10.0) < 1e-9
         assert b["k_lo"] <= b["plain"] < max(b["k_hi"], 2.0)
+
+
+def test_symmetry_images_transform_features_and_targets_together():
+    """Each image is one element of the cube's symmetry group applied to a sample: the
+    scalar features and the temperature target are unchanged; offsets about the cell
+    centre, the slip direction and the velocity target permute and change sign together,
+    so every dot product among them and every norm is kept; the images cover the group."""
+    rng = np.random.default_rng(11)
+    m = 400
+    f = np.column_stack([rng.uniform(0, 1, (m, 3)), rng.normal(size=(m, 3)), rng.uniform(size=(m, 4))])
+    y = rng.normal(size=(m, 4))
+    F, Y = learn.symmetry_images(f, y, 5, 1)
+    assert F.shape == (6 * m, 10) and Y.shape == (6 * m, 4)
+    assert np.array_equal(F[:m], f) and np.array_equal(Y[:m], y)
+    seen = set()
+    for c in range(1, 6):
+        g, z = F[c * m:(c + 1) * m], Y[c * m:(c + 1) * m]
+        assert np.array_equal(g[:, 6:], f[:, 6:]) and np.array_equal(z[:, 3], y[:, 3])
+        vecs_f = (f[:, :3] - 0.5, f[:, 3:6], y[:, :3])
+        vecs_g = (g[:, :3] - 0.5, g[:, 3:6], z[:, :3])
+        for a in range(3):
+            for b in range(3):
+                assert np.allclose(np.sum(vecs_g[a] * vecs_g[b], 1), np.sum(vecs_f[a] * vecs_f[b], 1))
+        assert np.all((g[:, :3] >= 0) & (g[:, :3] <= 1))
+        # which group element: the signed permutation mapping d to its image
+        for i in range(0, m, 7):
+            M = np.round(np.linalg.lstsq(np.stack([f[i, 3:6], y[i, :3], f[i, :3] - 0.5]),
+                                         np.stack([g[i, 3:6], z[i, :3], g[i, :3] - 0.5]), rcond=None)[0], 6)
+            assert np.allclose(np.abs(M).sum(0), 1) and np.allclose(np.abs(M).sum(1), 1)
+            seen.add(tuple(M.ravel()))
+    assert len(seen) > 30  # of 48
+    assert learn.symmetry_images(f, y, 0, 1)[0] is f
