@@ -304,12 +304,13 @@ def symmetry_images(f: np.ndarray, y: np.ndarray, copies: int, seed: int) -> tup
 
 
 def train(f: np.ndarray, y: np.ndarray, steps: int = 20000, batch: int = 8192, lr: float = 1e-3, seed: int = 0,
-          emphasis: float = 0.0, symmetries: int = 0):
+          emphasis: float = 0.0, symmetries: int = 0, decay: float = 0.0):
     """Adam on the mean squared error of the targets in units of the prior. emphasis > 0 draws
     the training rows with probability proportional to prior ** emphasis (seeded), so that the
     particles with the largest disturbance per unit slip -- whose error dominates the
     self-induced slip error -- weigh more. symmetries > 0 adds that many images of every
-    sample under the box's symmetries (symmetry_images)."""
+    sample under the box's symmetries (symmetry_images). decay > 0 runs that fraction of the
+    steps, at the end, at lr / 10 (Adam's moments carry over)."""
     f, y = symmetry_images(f, y, symmetries, seed + 29)
     shift, scale, lo, hi = normaliser(f)
     pr = prior(f)
@@ -323,7 +324,10 @@ def train(f: np.ndarray, y: np.ndarray, steps: int = 20000, batch: int = 8192, l
     # difference give meaningless ratios, which are clipped
     yt = np.clip(y / pr[:, None], -TARGET_CLIP, TARGET_CLIP)
     net.set_data(x, yt.astype(np.float32))
-    loss = net.train(steps, batch=batch, lr=lr, seed=seed + 1)
+    late = int(round(steps * decay))
+    loss = net.train(steps - late, batch=batch, lr=lr, seed=seed + 1)
+    if late:
+        loss = np.concatenate([loss, net.train(late, batch=batch, lr=lr * 0.1, seed=seed + 2)])
     model = dict(params=net.params, shift=shift.astype(np.float32), scale=scale.astype(np.float32),
                  lo=lo.astype(np.float32), hi=hi.astype(np.float32), prior_re=np.float32(PRIOR_RE))
     return model, loss, net
@@ -406,7 +410,8 @@ def load_model(path: str = MODEL_FILE) -> dict:
 
 def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, eval_runs: int | None = None,
              steps: int = 20000, batch: int = 8192, lr: float = 1e-3, eval_lattice: int = 32, rounds: int = 2,
-             emphasis: float = 0.0, drive_cap: float = 0.0, symmetries: int = 0, log=print) -> dict:
+             emphasis: float = 0.0, drive_cap: float = 0.0, symmetries: int = 0, decay: float = 0.0,
+             log=print) -> dict:
     """Generate the training set, train, and compare plain and corrected steps on held-out boxes.
 
     Data: the plain two-way-coupled runs, then `rounds` times the same boxes run with the
@@ -429,7 +434,7 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
     net_model = None
     for rnd in range(rounds):
         net_model, loss1, _ = train(np.concatenate(f_all), np.concatenate(y_all), steps=steps // 2, batch=batch, lr=lr,
-                                    seed=seed + 100 * rnd, emphasis=emphasis, symmetries=symmetries)
+                                    seed=seed + 100 * rnd, emphasis=emphasis, symmetries=symmetries, decay=decay)
         if drive_cap > 0:
             net_model["drive_cap"] = np.float32(drive_cap)
         log(f"round {rnd} network: loss {loss1[-100:].mean():.4e}")
@@ -441,7 +446,7 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
     f = np.concatenate(f_all)
     y = np.concatenate(y_all)
     model, loss, net = train(f, y, steps=steps, batch=batch, lr=lr, seed=seed + 7, emphasis=emphasis,
-                             symmetries=symmetries)
+                             symmetries=symmetries, decay=decay)
     if drive_cap > 0:
         model["drive_cap"] = np.float32(drive_cap)
     log(f"trained: loss {loss[:10].mean():.4e} -> {loss[-100:].mean():.4e}")
@@ -494,12 +499,14 @@ if __name__ == "__main__":
     ap.add_argument("--emphasis", type=float, default=0.0, help="draw training rows with probability prior**emphasis")
     ap.add_argument("--drive-cap", type=float, default=0.0, help="drive slip cap in units of the plain slip (0: 10)")
     ap.add_argument("--symmetries", type=int, default=0, help="images of each sample under the box's symmetries")
+    ap.add_argument("--decay", type=float, default=0.0, help="fraction of the steps run at lr/10 at the end")
     ap.add_argument("--out", default=MODEL_FILE)
     a = ap.parse_args()
-    r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis, drive_cap=a.drive_cap, symmetries=a.symmetries)
+    r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis, drive_cap=a.drive_cap, symmetries=a.symmetries,
+                 decay=a.decay)
     meta = {k: r[k] for k in ("plain", "corrected", "slip_reduction", "settle_reduction", "temp_reduction", "samples",
                               "final_loss", "boxes", "slip_by_k")}
     meta["settings"] = {"steps": a.steps, "rounds": a.rounds, "emphasis": a.emphasis, "drive_cap": a.drive_cap,
-                        "symmetries": a.symmetries}
+                        "symmetries": a.symmetries, "decay": a.decay}
     save_model(r["model"], a.out, meta)
     print(json.dumps(meta))

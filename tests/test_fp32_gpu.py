@@ -37,12 +37,28 @@ def run_pair(name, steps=None):
     g.bind_temperature(tf)
     o.prime(tf)
     g.prime()
-    errs = []
+    errs, parts = [], []
     for _ in range(steps):
         o.run(1, ux, uy, uz, tf)
         g.run(1)
         errs.append(compare(o, g, bp.l))
-    return errs, g
+        parts.append(per_particle(o, g, bp.l, cdef["n"]))
+    return errs, g, parts
+
+
+def per_particle(o, g, L, n):
+    """Per-particle errors of the FP32 form against the oracle: positions in cells (the
+    largest component), velocity vectors and temperatures relative to their own size."""
+    fo, fg = o.flag(), g.array("flag")
+    io, ig = np.argsort(fo), np.argsort(fg)
+    dpos = np.stack([(g.array(k)[ig] - o.array(k)[io] + L / 2) % L - L / 2 for k in ("x", "y", "z")], 1)
+    cells = np.max(np.abs(dpos), 1) * n / L
+    vo = np.stack([o.array(k)[io] for k in ("u", "v", "w")], 1)
+    vg = np.stack([g.array(k)[ig] for k in ("u", "v", "w")], 1)
+    vel = np.linalg.norm(vg - vo, axis=1) / np.maximum(np.linalg.norm(vo, axis=1), 1e-300)
+    to = o.array("T")[io]
+    temp = np.abs(g.array("T")[ig] - to) / np.maximum(np.abs(to), 1e-300)
+    return {"position_cells": cells, "velocity_rel": vel, "temperature_rel": temp}
 
 
 def compare(o, g, L):
@@ -78,10 +94,13 @@ def compare(o, g, L):
 
 @pytest.mark.parametrize("name", ["box16_twc_off_gravity", "box32_clustered", "box64_uniform"])
 def test_fp32_error_against_fp64_oracle(built_cuda, name):
-    errs, g = run_pair(name, steps=3)
+    errs, g, parts = run_pair(name, steps=3)
     for step, e in enumerate(errs):
         bad = {k: v for k, v in e.items() if not v <= REL_TOL}
         assert not bad, f"step {step}: {bad}"
+    report = [{k: {"max": float(v.max()), "p99.9": float(np.quantile(v, 0.999))} for k, v in p.items()}
+              for p in parts]
+    print(name, "per-particle FP32 error after each step:", report)
     rc, flags = g.check()
     assert rc == 0, flags
 
