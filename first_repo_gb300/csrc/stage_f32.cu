@@ -108,6 +108,8 @@ struct F32Form {
   int32_t *sidx;
   uint32_t *bounds;   // [0..2] max |RHS_u| per component (float bits), [3] max |RHS_T|, [4] max per-cell count
   uint32_t *slots;    // kBoundSlots x 4 partial maxima (spread so blocks do not contend on one word)
+  uint32_t *pslots;   // kBoundSlots x 2: the last stage's max u and max ug (order-preserving keys)
+  int pmax_state;     // 0: none; 1: filled by this step's last stage; 2: valid for the base state
   int32_t *se;        // fixed-point scale exponents per field
   unsigned long long *totals;  // exact integer sums, maxima, minima of the five fields (last deposit)
   double *fstat;               // per field: max, min, interior sum as fp64 (k_totals)
@@ -180,6 +182,31 @@ __device__ inline void block_max4(uint32_t *slots, float a0, float a1, float a2,
     float m = 0.f;
     for (int q = 0; q < nw; ++q) m = fmaxf(m, red[threadIdx.x][q]);
     atomic_max_abs(&slots[(blockIdx.x % kBoundSlots) * 4 + threadIdx.x], m);
+  }
+}
+
+// order-preserving 32-bit key of a float (larger float, larger key; 0 is below every key)
+__device__ __forceinline__ uint32_t order_key(float v) {
+  const uint32_t b = __float_as_uint(v);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// block maximum of 2 signed values into slot blockIdx % kBoundSlots as order keys (a block
+// with no particle leaves its slots alone)
+__device__ inline void block_max2_signed(uint32_t *slots, float a0, float a1) {
+  __shared__ float red2[2][32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 = fmaxf(a0, __shfl_xor_sync(0xffffffffu, a0, o));
+    a1 = fmaxf(a1, __shfl_xor_sync(0xffffffffu, a1, o));
+  }
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0) { red2[0][w] = a0; red2[1][w] = a1; }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    float m = -INFINITY;
+    for (int q = 0; q < nw; ++q) m = fmaxf(m, red2[threadIdx.x][q]);
+    if (m > -INFINITY) atomicMax(&slots[(blockIdx.x % kBoundSlots) * 2 + threadIdx.x], order_key(m));
   }
 }
 
@@ -365,14 +392,18 @@ template <int K>
 __global__ void __launch_bounds__(256) k_advance32(Geom G, F32Form f, C32 c, int twc, int64_t n,
                                                    int32_t *__restrict__ err) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
+  float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f, umax = -INFINITY, gmax = -INFINITY;
   if (p < n) {
     Adv a;
     adv_load<K>(G, f, c, p, a);
     adv_finish<K>(G, f, c, twc, p, a, err, mu0, mu1, mu2, mt);
+    umax = a.vac[0];
+    gmax = a.gas[0];
   }
   // bounds for the fixed-point scales (order-independent maxima)
   block_max4(f.slots, mu0, mu1, mu2, mt);
+  // the last stage: max u of the step's result and max ug (grid.cpp:726-727)
+  if (K == 3) block_max2_signed(f.pslots, umax, gmax);
 }
 
 // ----------------------------------------------------------------------------
@@ -698,7 +729,7 @@ template <int K>
 __global__ void __launch_bounds__(256, 5) k_advance32_corr(Geom G, F32Form f, C32 c, int twc, int64_t n,
                                                         int32_t *__restrict__ err, CorrDev cd) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f;
+  float mu0 = 0.f, mu1 = 0.f, mu2 = 0.f, mt = 0.f, umax = -INFINITY, gmax = -INFINITY;
   if (p < n) {
     Adv a;
     adv_load<K>(G, f, c, p, a);
@@ -721,8 +752,11 @@ __global__ void __launch_bounds__(256, 5) k_advance32_corr(Geom G, F32Form f, C3
     const float dv[3] = {a.vin[0] - a.gas[0], a.vin[1] - a.gas[1], a.vin[2] - a.gas[2]};
     const float dt_drive = adv_finish_mlp<K>(G, f, c, twc, p, a, ty, td, err, mu0, mu1, mu2, mt);
     f.drive[p] = make_uint2(pack_bf16x2(dv[0], dv[1]), pack_bf16x2(dv[2], dt_drive));
+    umax = a.vac[0];
+    gmax = a.gas[0];
   }
   block_max4(f.slots, mu0, mu1, mu2, mt);
+  if (K == 3) block_max2_signed(f.pslots, umax, gmax);
 }
 
 // the prime (grid.cpp:223-226) at the base positions: Tg, RHS_T
@@ -1634,6 +1668,8 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->bounds, 8));
   TRY32(dalloc32(h, f->slots, kBoundSlots * 4));
   PSTEP_CUDA(cudaMemsetAsync(f->slots, 0, kBoundSlots * 4 * sizeof(uint32_t), h->stream));
+  TRY32(dalloc32(h, f->pslots, kBoundSlots * 2));
+  f->pmax_state = 0;
   TRY32(dalloc32(h, f->se, 8));
   TRY32(dalloc32(h, f->totals, 16));
   TRY32(dalloc32(h, f->fstat, 16));
@@ -1659,7 +1695,7 @@ int f32_destroy(pstep_ctx *h) {
   dfree32(f->corr_y);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx);
-  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots); dfree32(f->totals); dfree32(f->fstat);
+  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots); dfree32(f->pslots); dfree32(f->totals); dfree32(f->fstat);
   {
     Work &w = f->work;
     dfree32(w.items); dfree32(w.nchunk); dfree32(w.slot); dfree32(w.cnt_a); dfree32(w.cnt_b); dfree32(w.cnt_s);
@@ -1702,6 +1738,7 @@ int f32_upload(pstep_ctx *h, const double *x, const double *y, const double *z, 
   if (f.drive) PSTEP_CUDA(cudaMemsetAsync(f.drive, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   if (f.corr_y) PSTEP_CUDA(cudaMemsetAsync(f.corr_y, 0, sizeof(uint2) * (size_t)h->cap, h->stream));
   f.sorted = 0;
+  f.pmax_state = 0;
   if (n == 0) return PSTEP_OK;
   if (!f.tref_set) {
     double t0 = 0.0;
@@ -1937,6 +1974,12 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
     PSTEP_LAUNCHED(h);
     prof_end(h, PSTEP_PHASE_NETWORK);
   }
+  if (k == 3) {  // the last stage gathers the step result's max u and max ug
+    PSTEP_CUDA(cudaMemsetAsync(f.pslots, 0, sizeof(uint32_t) * kBoundSlots * 2, h->stream));
+    f.pmax_state = 1;
+  } else if (f.pmax_state == 1) {
+    f.pmax_state = 0;  // a stage after the last one without the step's end
+  }
   prof_begin(h, PSTEP_PHASE_ADVANCE);
   if (n > 0 && h->corr_on) {
     switch (k) {
@@ -2026,6 +2069,26 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
 }
 }  // namespace
 
+// particle::max of u or ug (grid.cpp:726-727) as the last stage gathered them, when they
+// describe the current base state (the step's result): PSTEP_OK with *out set, or -1
+// when they are not available (the caller then makes a pass over the array)
+int f32_fused_max(pstep_ctx *h, int id, double *out) {
+  F32Form &f = *h->f32;
+  if (f.pmax_state != 2 || (id != PSTEP_U && id != PSTEP_UG)) return -1;
+  uint32_t keys[kBoundSlots * 2];
+  PSTEP_CUDA(cudaMemcpyAsync(keys, f.pslots, sizeof keys, cudaMemcpyDeviceToHost, h->stream));
+  PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+  const int q = id == PSTEP_U ? 0 : 1;
+  uint32_t best = 0;
+  for (int s = 0; s < kBoundSlots; ++s) best = keys[2 * s + q] > best ? keys[2 * s + q] : best;
+  if (best == 0) return -1;
+  const uint32_t bits = (best & 0x80000000u) ? (best & 0x7fffffffu) : ~best;
+  float v;
+  memcpy(&v, &bits, sizeof v);
+  *out = (double)v;
+  return PSTEP_OK;
+}
+
 // device address of a deposited field's max, min and interior sum of the last deposit
 // that wrote it (FP32 form)
 const double *f32_field_stats_dev(pstep_ctx *h, int field) { return h->f32->fstat + 3 * field; }
@@ -2040,6 +2103,7 @@ int f32_end_stage(pstep_ctx *h) {
 
 int f32_end_step(pstep_ctx *h) {
   F32Form &f = *h->f32;
+  f.pmax_state = f.pmax_state == 1 ? 2 : 0;  // the last stage's maxima describe the new base
   Set32 t = f.set[SBASE];
   f.set[SBASE] = f.set[SNP1];
   f.set[SNP1] = t;

@@ -121,3 +121,35 @@ def test_fp32_snapshot_round_trip_and_statistics(built_cuda, tmp_path):
     assert e.value.status == 11
     g.close()
     g2.close()
+
+
+def test_fp32_particle_maxima_fused_into_the_last_stage(built_cuda):
+    """grid::Statistics' particle maxima (grid.cpp:726-727: max u and max ug) come out of
+    the FP32 step's last stage without a pass over the particles: pstep_max launches no
+    kernel then, and equals the maximum of the arrays the step left (ug kept with
+    PSTEP_KEEP_GAS here to compare), plain and with the learned correction. After an
+    upload (no step yet) the call falls back to a pass."""
+    from first_repo_gb300 import learn
+    case = gen.make_case(N, COUNT, 23, True)
+    bp = helpers.make_bp(N, COUNT)
+    arrs = [np.ascontiguousarray(case[k]) for k in ("x", "y", "z", "u", "v", "w", "t", "flag")]
+    ux, uy, uz, tf = helpers.ghosted_fields(case)
+    for corrected in (False, True):
+        g = pstep.ParticleStep(bp.step_config(), COUNT, pstep.FP32, pstep.KEEP_GAS)
+        g.load(*arrs)
+        if corrected:
+            g.set_correction(learn.load_model(), bp.mu0 / bp.rho0)
+        g.bind_velocity(ux, uy, uz)
+        g.bind_temperature(tf)
+        g.prime()
+        before = g.launches()
+        assert g.max("u") == float(np.max(g.array("u")))  # after the upload: a pass
+        assert g.launches() > before
+        g.run(2)
+        for name in ("u", "ug"):
+            before = g.launches()
+            got = g.max(name)
+            assert g.launches() == before, name  # read from the last stage's epilogue
+            assert got == float(np.max(g.array(name))), (corrected, name)
+        assert g.max("v") == float(np.max(g.array("v")))  # other arrays: a pass
+        g.close()
