@@ -563,21 +563,25 @@ def main():
             g.download(*dev_out)
             ev_out.record(main_s)
             # the particles through the host copy, array by array: each array goes up as
-            # soon as it is down, the two directions overlapping; then the deposited fields
+            # soon as it is down, the two directions overlapping; the deposited fields come
+            # down once the particles are back up (while the next step computes), so they
+            # do not take link bandwidth from the particles' round trip
             with torch.cuda.stream(down_s):
                 down_s.wait_event(ev_out)
                 for a in range(len(hpart)):
                     hpart[a].copy_(dev_out[a], non_blocking=True)
                     ev_arr[a].record(down_s)
-                down_s.wait_event(ev_dep_ready)
-                for i in range(5):
-                    out_f[i].copy_(dev_dep[i], non_blocking=True)
-                ev_dep_free.record(down_s)
             with torch.cuda.stream(up_s):
                 for a in range(len(hpart)):
                     up_s.wait_event(ev_arr[a])
                     dev_in[a].copy_(hpart[a], non_blocking=True)
                 ev_in.record(up_s)
+            with torch.cuda.stream(down_s):
+                down_s.wait_event(ev_in)
+                down_s.wait_event(ev_dep_ready)
+                for i in range(5):
+                    out_f[i].copy_(dev_dep[i], non_blocking=True)
+                ev_dep_free.record(down_s)
             slot[0] = 1 - sl
 
         with torch.cuda.stream(up_s):

@@ -411,7 +411,7 @@ def load_model(path: str = MODEL_FILE) -> dict:
 def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, eval_runs: int | None = None,
              steps: int = 20000, batch: int = 8192, lr: float = 1e-3, eval_lattice: int = 32, rounds: int = 2,
              emphasis: float = 0.0, drive_cap: float = 0.0, symmetries: int = 0, decay: float = 0.0,
-             log=print) -> dict:
+             closed_only: bool = False, log=print) -> dict:
     """Generate the training set, train, and compare plain and corrected steps on held-out boxes.
 
     Data: the plain two-way-coupled runs, then `rounds` times the same boxes run with the
@@ -443,6 +443,11 @@ def pipeline(spec: Spec | None = None, seed: int = 3001, eval_seed: int = 4001, 
             f_all.append(f)
             y_all.append(y)
         log(f"round {rnd}: closed-loop samples from {len(runs)} boxes")
+    if closed_only and rounds > 0:
+        # the final network on the closed-loop rounds alone: in the plain runs the drag slip
+        # falls as the disturbance builds up, so the disturbance per unit of the current
+        # slip carries the force's history; the corrected step holds the slip steady
+        f_all, y_all = f_all[len(runs):], y_all[len(runs):]
     f = np.concatenate(f_all)
     y = np.concatenate(y_all)
     model, loss, net = train(f, y, steps=steps, batch=batch, lr=lr, seed=seed + 7, emphasis=emphasis,
@@ -500,13 +505,14 @@ if __name__ == "__main__":
     ap.add_argument("--drive-cap", type=float, default=0.0, help="drive slip cap in units of the plain slip (0: 10)")
     ap.add_argument("--symmetries", type=int, default=0, help="images of each sample under the box's symmetries")
     ap.add_argument("--decay", type=float, default=0.0, help="fraction of the steps run at lr/10 at the end")
+    ap.add_argument("--closed-only", action="store_true", help="final network on the closed-loop rounds' data only")
     ap.add_argument("--out", default=MODEL_FILE)
     a = ap.parse_args()
     r = pipeline(steps=a.steps, rounds=a.rounds, emphasis=a.emphasis, drive_cap=a.drive_cap, symmetries=a.symmetries,
-                 decay=a.decay)
+                 decay=a.decay, closed_only=a.closed_only)
     meta = {k: r[k] for k in ("plain", "corrected", "slip_reduction", "settle_reduction", "temp_reduction", "samples",
                               "final_loss", "boxes", "slip_by_k")}
     meta["settings"] = {"steps": a.steps, "rounds": a.rounds, "emphasis": a.emphasis, "drive_cap": a.drive_cap,
-                        "symmetries": a.symmetries, "decay": a.decay}
+                        "symmetries": a.symmetries, "decay": a.decay, "closed_only": a.closed_only}
     save_model(r["model"], a.out, meta)
     print(json.dumps(meta))
