@@ -139,6 +139,7 @@ void release(pstep_ctx *h) {
   dfree(h->own_t);
   for (int f = 0; f < PSTEP_NUM_FIELDS; ++f) dfree(h->dep[f]);
   dfree(h->emean_dev); dfree(h->mom_dev); dfree(h->red_partials);
+  dfree(h->pmax64);
   dfree(h->ref_of_phys); dfree(h->phys_of_ref); dfree(h->leave_code); dfree(h->ord_scratch); dfree(h->ord_count);
   dfree(h->err_word);
   if (is_f32(h)) f32_destroy(h);
@@ -166,6 +167,7 @@ int alloc_all(pstep_ctx *h) {
     }
     TRY(dalloc(h, h->s.key_prev, cap)); TRY(dalloc(h, h->s.key_new, cap));
     TRY(dalloc(h, h->csr_prev.sidx, cap)); TRY(dalloc(h, h->csr_new.sidx, cap));
+    TRY(dalloc(h, h->pmax64, 2 * 1024));
     if (h->cfg.flags & PSTEP_TRACK_ORDER) {
       TRY(dalloc(h, h->ref_of_phys, cap)); TRY(dalloc(h, h->phys_of_ref, cap));
       TRY(dalloc(h, h->leave_code, cap));
@@ -338,6 +340,7 @@ int pstep_upload_particles(pstep_handle h, int64_t n, const double *x, const dou
   h->np = n;
   h->primed = 0;
   h->phase = 0;
+  h->pmax64_state = 0;
   if (is_f32(h)) {
     TRY(f32_upload(h, x, y, z, u, v, w, t, on_device));
   } else {
@@ -481,6 +484,10 @@ int pstep_stage_interp_advance_deposit(pstep_handle h, int k, double pre, double
     return PSTEP_OK;
   }
   h->fields_t_at_advance = h->fields_t;
+  if (k == 3) {  // the last stage gathers the step result's max u and max ug
+    PSTEP_CUDA(cudaMemsetAsync(h->pmax64, 0, sizeof(unsigned long long) * 2 * 1024, h->stream));
+    h->pmax64_state = 1;
+  }
   prof_begin(h, PSTEP_PHASE_ADVANCE);
   TRY(f64_advance(h, k, pre, post));
   prof_end(h, PSTEP_PHASE_ADVANCE);
@@ -554,6 +561,7 @@ int pstep_end_step(pstep_handle h) {
   } else {
     // base = np1 (TimeAdvance); then reorder storage by the cell sort of these positions
     for (int q = 0; q < 7; ++q) { double *t = h->s.base[q]; h->s.base[q] = h->s.np1[q]; h->s.np1[q] = t; }
+    h->pmax64_state = h->pmax64_state == 1 ? 2 : 0;  // the last stage's maxima describe the new base
     prof_begin(h, PSTEP_PHASE_REORDER);
     TRY(f64_reorder(h));
     prof_end(h, PSTEP_PHASE_REORDER);

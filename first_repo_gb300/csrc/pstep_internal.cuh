@@ -115,6 +115,8 @@ struct pstep_ctx {
   // reference-order bookkeeping
   int32_t *ref_of_phys, *phys_of_ref;
   uint8_t *leave_code;      // per particle: bit 2d = high side, bit 2d+1 = low side, dimension d
+  unsigned long long *pmax64;  // FP64 form: 1024 x 2 order keys of the last stage's max u and max ug
+  int pmax64_state;            // 0: none; 1: filled by this step's last stage; 2: valid for the base state
   int32_t *leavers;         // compaction scratch
   uint32_t *bitmap;         // n bits
   int32_t *ord_scratch;     // misc scratch for the order passes
@@ -184,6 +186,7 @@ int momentum_sums(pstep_ctx *h);
 int f32_download(pstep_ctx *h, double *const dst[7], int32_t *flag, int on_device);
 const double *f32_field_stats_dev(pstep_ctx *h, int field);
 int f32_fused_max(pstep_ctx *h, int id, double *out);
+int f64_fused_max(pstep_ctx *h, int id, double *out);
 int order_passes(pstep_ctx *h);
 int order_init(pstep_ctx *h);
 int order_permute(pstep_ctx *h, const int32_t *sidx);

@@ -94,13 +94,28 @@ __global__ void k_prime(Geom G, F64State s, const double *__restrict__ T, double
   s.key_new[i] = node_key(G, r);
 }
 
+// order-preserving 64-bit key of a double (larger double, larger key; 0 is below every key)
+__device__ __forceinline__ unsigned long long order_key64(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | (1ull << 63));
+}
+
+// warp maximum of 64-bit keys over the warp's active lanes (two 32-bit reductions)
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned mask, unsigned long long k) {
+  const unsigned hi = (unsigned)(k >> 32);
+  const unsigned mh = __reduce_max_sync(mask, hi);
+  const unsigned ml = __reduce_max_sync(mask, hi == mh ? (unsigned)k : 0u);
+  return ((unsigned long long)mh << 32) | ml;
+}
+
 // One RK4 stage for every particle (particle.cpp:314-399, 480-496, 58-104, 430-478).
 // Reads the stage's x_int record (fraction + key, computed when x_int was made).
 template <int K>
 __global__ void __launch_bounds__(kThreads) k_advance(Geom G, F64State s, StageConst c, const double *__restrict__ Ux,
                                                       const double *__restrict__ Uy, const double *__restrict__ Uz,
                                                       const double *__restrict__ T, int twc, int64_t n,
-                                                      uint8_t *__restrict__ leave, int32_t *__restrict__ err) {
+                                                      uint8_t *__restrict__ leave, int32_t *__restrict__ err,
+                                                      unsigned long long *__restrict__ pmax) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   // stage inputs: at k = 0 the *_int and *_np1 values equal the base state
@@ -204,6 +219,17 @@ __global__ void __launch_bounds__(kThreads) k_advance(Geom G, F64State s, StageC
   }
   s.rhs_t[i] = rhs_t_new;
   s.key_new[i] = node_key(G, r);
+  // the last stage: max u of the step's result and max ug (grid.cpp:726-727), per warp
+  // into one of 1024 slot pairs
+  if (K == 3 && pmax) {
+    const unsigned mask = __activemask();
+    const unsigned long long ku = warp_max_key(mask, order_key64(acc[3])), kg = warp_max_key(mask, order_key64(ug));
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) {
+      const int slot = (int)((((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) % 1024);
+      atomicMax(&pmax[2 * slot], ku);
+      atomicMax(&pmax[2 * slot + 1], kg);
+    }
+  }
 }
 
 // gas2part_Temp_new + Compute_RHS_Temp_new from the x_new record, for a temperature
@@ -264,7 +290,7 @@ int f64_advance(pstep_ctx *h, int k, double pre, double post) {
   const int twc = h->cfg.twc;
 #define PSTEP_ADV(KK)                                                                                   \
   k_advance<KK><<<blocks, kThreads, 0, h->stream>>>(h->geom, h->s, c, h->ux, h->uy, h->uz, h->tf, twc, \
-                                                    h->np, leave, h->err_word)
+                                                    h->np, leave, h->err_word, h->pmax64)
   switch (k) {
     case 0: PSTEP_ADV(0); break;
     case 1: PSTEP_ADV(1); break;
@@ -279,6 +305,22 @@ int f64_advance(pstep_ctx *h, int k, double pre, double post) {
 }  // namespace pstep
 
 namespace pstep {
+// particle::max of u or ug (grid.cpp:726-727) as the FP64 form's last stage gathered
+// them, when they describe the current base state: PSTEP_OK with *out set, or -1
+int f64_fused_max(pstep_ctx *h, int id, double *out) {
+  if (h->pmax64_state != 2 || !h->pmax64 || (id != PSTEP_U && id != PSTEP_UG)) return -1;
+  unsigned long long keys[2 * 1024];
+  PSTEP_CUDA(cudaMemcpyAsync(keys, h->pmax64, sizeof keys, cudaMemcpyDeviceToHost, h->stream));
+  PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+  const int q = id == PSTEP_U ? 0 : 1;
+  unsigned long long best = 0;
+  for (int s = 0; s < 1024; ++s) best = keys[2 * s + q] > best ? keys[2 * s + q] : best;
+  if (best == 0) return -1;
+  const unsigned long long bits = (best >> 63) ? (best & ~(1ull << 63)) : ~best;
+  memcpy(out, &bits, sizeof bits);
+  return PSTEP_OK;
+}
+
 int f64_temp_gather(pstep_ctx *h) {
   if (h->np == 0) return PSTEP_OK;
   StageConst c = make_stage_const(h->cfg, 0, 0.5, 1. / 6.);

@@ -174,9 +174,9 @@ int pstep_max(pstep_handle h, int id, double *out) {
     *out = -1e9;  // particle.cpp:674
     return PSTEP_OK;
   }
-  if (h->f32) {
-    // the FP32 form's last stage gathers max u and max ug in its epilogue
-    const int fr = f32_fused_max(h, id, out);
+  {
+    // the last stage gathers max u and max ug in its epilogue
+    const int fr = h->f32 ? f32_fused_max(h, id, out) : f64_fused_max(h, id, out);
     if (fr != -1) return fr;
   }
   double *vals = nullptr, *part = nullptr;

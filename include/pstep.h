@@ -312,10 +312,11 @@ int64_t pstep_launch_count(pstep_handle h);
 int pstep_np_tot(pstep_handle h, int64_t *out);
 /* particle::max (particle.cpp:671-685) of one particle array (PSTEP_X ... PSTEP_TG, not
  * PSTEP_FLAG), as pstep_get_particle_array would return it: its largest value, or -1e9
- * when there are no particles. PSTEP_FP32, after pstep_end_step (or pstep_run): the
+ * when there are no particles. After pstep_end_step (or pstep_run), both forms: the
  * maxima of u and ug that grid::Statistics asks for (grid.cpp:726-727) are gathered by
  * the step's last stage in its epilogue, so PSTEP_U and PSTEP_UG read them without a
- * pass over the particles (PSTEP_UG then needs no PSTEP_KEEP_GAS); other arrays, and
+ * pass over the particles (PSTEP_UG then needs no PSTEP_KEEP_GAS, and the FP64 form,
+ * which keeps no per-particle gas values, answers it only this way); other arrays, and
  * any state not left by a full step, take a pass. */
 int pstep_max(pstep_handle h, int id, double *out);
 /* particle::Balance_Index (particle.cpp:730-741): largest over smallest per-rank particle

@@ -67,6 +67,12 @@ def test_fp64_store_all_is_the_reference_files(built_cuda, tmp_path):
     assert g.balance_index() == 1.0
     for k in KEYS:
         assert g.max(k) == pyoracle.array_max(o.array(k)), k
+    # max u and max ug (grid::Statistics) come from the last stage's epilogue: no kernel
+    # launch, equal to the oracle's (its ug is the gas velocity of the last stage)
+    before = g.launches()
+    assert g.max("u") == pyoracle.array_max(o.array("u"))
+    assert g.max("ug") == pyoracle.array_max(o.array("ug"))
+    assert g.launches() == before
     _check_field_stats(g)
     for name, key in (("C", "C"), ("RHS_Part_Temp", "E")):  # the oracle's fields, within the deposit bound
         mx, mn, me = g.field_stats(name)
@@ -125,7 +131,8 @@ def test_fp32_snapshot_round_trip_and_statistics(built_cuda, tmp_path):
 
 def test_fp32_particle_maxima_fused_into_the_last_stage(built_cuda):
     """grid::Statistics' particle maxima (grid.cpp:726-727: max u and max ug) come out of
-    the FP32 step's last stage without a pass over the particles: pstep_max launches no
+    the FP32 step's last stage without a pass over the particles (the FP64 form's are
+    checked against the oracle above): pstep_max launches no
     kernel then, and equals the maximum of the arrays the step left (ug kept with
     PSTEP_KEEP_GAS here to compare), plain and with the learned correction. After an
     upload (no step yet) the call falls back to a pass."""
