@@ -408,7 +408,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--c4-steps", type=int, default=100,
                     help="steps after which the corrected step's slip and temperature statistics are compared with "
-                         "the FP64 drop-in's (untimed; needs the FP64 line)")
+                         "the FP64 drop-in's (untimed; needs the FP64 line; one GPU only, so that a multi-GPU run "
+                         "holds its GPUs no longer than its timing needs)")
     args = ap.parse_args()
     wl = config.WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -510,7 +511,7 @@ def main():
     # here, untimed), compared below with the plain FP64 drop-in after as many steps
     stats_steps = args.warmup + args.steps
     c4_extra = 0
-    if form == pstep.FP32 and not args.no_fp64_line and args.c4_steps > stats_steps:
+    if form == pstep.FP32 and not args.no_fp64_line and args.c4_steps > stats_steps and world == 1:
         c4_extra = args.c4_steps - stats_steps
         g.run(c4_extra)
         stats_steps = args.c4_steps
