@@ -830,6 +830,15 @@ __global__ void k_max_count(const int32_t *__restrict__ cs, int64_t ncell, uint3
 // exact conversion of a scaled 64-bit integer sum q * 2^-se to fp64 with integer operations
 __device__ inline double fixed_to_f64(long long q, int se) {
   if (q == 0) return 0.0;
+  if (q == (long long)(int)q) {  // |q| < 2^31: the same steps in 32-bit operations, exact (no rounding)
+    const unsigned sgn = q < 0 ? 1u : 0u;
+    unsigned m = (unsigned)(sgn ? -q : q);
+    const int lz = __clz(m);
+    m <<= lz;  // leading one at bit 31: value = (m / 2^31) * 2^(31 - lz - se)
+    const int ex = 31 - lz - se + 1023;
+    if (ex <= 0) return 0.0;
+    return __hiloint2double((int)((sgn << 31) | ((unsigned)ex << 20) | ((m >> 11) & 0xfffffu)), (int)(m << 21));
+  }
   unsigned long long sgn = q < 0 ? 1ull : 0ull;
   unsigned long long m = sgn ? (unsigned long long)(-q) : (unsigned long long)q;
   int lz = __clzll(m);
@@ -1156,10 +1165,9 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
     brick_origin<BR, BZ>(G, brick, bx, by, bz);
     const int slot_idx = nch > 1 ? w.slot[brick] : -1;
     long long *tile = slot_idx >= 0 ? w.tiles + (int64_t)slot_idx * 5 * NB : nullptr;
-    for (int s = threadIdx.x; s < NF * SLOTS; s += blockDim.x) {
-      acc_lo[s] = 0u;
-      acc_hi[s] = 0u;
-    }
+    static_assert((2 * NF * SLOTS) % 4 == 0, "whole 16-byte vectors");
+    for (int s = threadIdx.x; s < 2 * NF * SLOTS / 4; s += blockDim.x)
+      reinterpret_cast<uint4 *>(acc_lo)[s] = make_uint4(0u, 0u, 0u, 0u);  // the lo and hi words, contiguous
     for (int r = threadIdx.x; r < NR; r += blockDim.x) {
       uint32_t id;
       int len;
