@@ -177,6 +177,7 @@ int f64_reorder(pstep_ctx *h);
 int sort_by_node(pstep_ctx *h, const uint32_t *keys, Csr &out);
 int csr_sort(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, const int32_t *order, int32_t *cell_start,
              int32_t *sidx, int order_within);
+int csr_count(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, int32_t *cell_start);
 template <typename T>
 __global__ void k_gather(const T *__restrict__ src, const int32_t *__restrict__ idx, int64_t n, T *__restrict__ dst);
 int fold_cum(pstep_ctx *h, double *f);

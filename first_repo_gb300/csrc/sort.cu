@@ -311,6 +311,17 @@ int csr_sort(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, const
   return PSTEP_OK;
 }
 
+// the cell-start table of keys already in non-decreasing order (no permutation needed):
+// the counts and their exclusive scan, as csr_sort makes them
+int csr_count(pstep_ctx *h, const uint32_t *keys, int shift, int64_t nkeys, int32_t *cell_start) {
+  PSTEP_CUDA(cudaMemsetAsync(h->counts, 0, sizeof(int32_t) * nkeys, h->stream));
+  if (h->np > 0) {
+    k_count<<<blocks_for(h->np), kThreads, 0, h->stream>>>(keys, shift, h->np, h->counts);
+    PSTEP_LAUNCHED(h);
+  }
+  return exclusive_scan(h, h->counts, nkeys, cell_start, nullptr);
+}
+
 int sort_by_node(pstep_ctx *h, const uint32_t *keys, Csr &out) {
   const int32_t *order =
       ((h->cfg.flags & PSTEP_TRACK_ORDER) && (h->cfg.flags & PSTEP_REFERENCE_SUMS)) ? h->ref_of_phys : nullptr;

@@ -110,6 +110,7 @@ struct F32Form {
   uint32_t *slots;    // kBoundSlots x 4 partial maxima (spread so blocks do not contend on one word)
   uint32_t *pslots;   // kBoundSlots x 2: the last stage's max u and max ug (order-preserving keys)
   int pmax_state;     // 0: none; 1: filled by this step's last stage; 2: valid for the base state
+  int32_t *unsorted;  // sort_step's storage-order test word
   int32_t *se;        // fixed-point scale exponents per field
   unsigned long long *totals;  // exact integer sums, maxima, minima of the five fields (last deposit)
   double *fstat;               // per field: max, min, interior sum as fp64 (k_totals)
@@ -1414,6 +1415,14 @@ __global__ void k_keys32(Geom G, Set32 S, int64_t n, uint32_t *__restrict__ key)
   key[p] = brick_id(G, ci_(c), cj_(c), ck_(c));
 }
 
+// any key above its successor: the storage is not in key order
+__global__ void k_keys_unsorted(const uint32_t *__restrict__ key, int64_t n, int32_t *__restrict__ flag) {
+  int unsorted = 0;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p + 1 < n; p += (int64_t)gridDim.x * blockDim.x)
+    unsorted |= key[p] > key[p + 1];
+  if (__syncthreads_or(unsorted) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 // Per-particle arrays gathered through the sort permutation, up to kPermBatch
 // arrays of one element type per launch: the permutation is read once per batch
 // and every thread keeps one independent load per array in flight (a gather of
@@ -1503,7 +1512,10 @@ void dfree32(T *&p) {
 
 int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN);
 
-int sort_step(pstep_ctx *h) {
+// check_sorted: first test whether the storage is in key order already (a population
+// uploaded as an earlier step left it, e.g. a host round trip), and then only build the
+// cell-start table; one 4-byte read-back
+int sort_step(pstep_ctx *h, bool check_sorted = false) {
   // particles by brick-major cell of the base position; storage reordered; per-cell CSR kept
   F32Form &f = *h->f32;
   const Geom &G = h->geom;
@@ -1513,10 +1525,23 @@ int sort_step(pstep_ctx *h) {
     k_keys32<<<nb(n), kThreads, 0, h->stream>>>(G, f.set[SBASE], n, f.key);
     PSTEP_LAUNCHED(h);
   }
+  bool in_order = false;
+  if (check_sorted && n > 1) {
+    PSTEP_CUDA(cudaMemsetAsync(f.unsorted, 0, sizeof(int32_t), h->stream));
+    k_keys_unsorted<<<h->num_sms * 8, kThreads, 0, h->stream>>>(f.key, n, f.unsorted);
+    PSTEP_LAUNCHED(h);
+    int32_t u = 1;
+    PSTEP_CUDA(cudaMemcpyAsync(&u, f.unsorted, sizeof u, cudaMemcpyDeviceToHost, h->stream));
+    PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+    in_order = u == 0;
+  }
   // The order inside a cell is left as the scatter makes it: every result of this form
   // (integer deposit sums, per-particle states by id) is independent of storage order.
-  TRY32(csr_sort(h, f.key, 0, ncell, h->s.flag, f.cell_start, f.sidx, 0));
-  if (n > 0) {
+  if (in_order)
+    TRY32(csr_count(h, f.key, 0, ncell, f.cell_start));
+  else
+    TRY32(csr_sort(h, f.key, 0, ncell, h->s.flag, f.cell_start, f.sidx, 0));
+  if (n > 0 && !in_order) {
     Set32 &B = f.set[SBASE];
     // every 4-byte per-particle array that lives across steps; the addresses of their
     // pointer fields (float *, uint32_t *, int32_t *), swapped through memcpy
@@ -1576,6 +1601,8 @@ int sort_step(pstep_ctx *h) {
       f.drive = f.corr_y;
       f.corr_y = t;
     }
+  }
+  if (n > 0) {
     PSTEP_CUDA(cudaMemsetAsync(&f.bounds[4], 0, sizeof(uint32_t), h->stream));
     k_max_count<<<1024, kThreads, 0, h->stream>>>(f.cell_start, ncell, &f.bounds[4]);
     PSTEP_LAUNCHED(h);
@@ -1677,6 +1704,7 @@ int f32_create(pstep_ctx *h) {
   TRY32(dalloc32(h, f->slots, kBoundSlots * 4));
   PSTEP_CUDA(cudaMemsetAsync(f->slots, 0, kBoundSlots * 4 * sizeof(uint32_t), h->stream));
   TRY32(dalloc32(h, f->pslots, kBoundSlots * 2));
+  TRY32(dalloc32(h, f->unsorted, 1));
   f->pmax_state = 0;
   TRY32(dalloc32(h, f->se, 8));
   TRY32(dalloc32(h, f->totals, 16));
@@ -1703,7 +1731,7 @@ int f32_destroy(pstep_ctx *h) {
   dfree32(f->corr_y);
   for (int d = 0; d < 3; ++d) { dfree32(f->rhs_u[d]); dfree32(f->uf[d]); }
   dfree32(f->tf); dfree32(f->key); dfree32(f->cell_start); dfree32(f->sidx);
-  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots); dfree32(f->pslots); dfree32(f->totals); dfree32(f->fstat);
+  dfree32(f->bounds); dfree32(f->se); dfree32(f->slots); dfree32(f->pslots); dfree32(f->unsorted); dfree32(f->totals); dfree32(f->fstat);
   {
     Work &w = f->work;
     dfree32(w.items); dfree32(w.nchunk); dfree32(w.slot); dfree32(w.cnt_a); dfree32(w.cnt_b); dfree32(w.cnt_s);
@@ -1952,7 +1980,7 @@ int f32_bind_fields(pstep_ctx *h, int which) {
 
 int f32_prime(pstep_ctx *h) {
   F32Form &f = *h->f32;
-  TRY32(sort_step(h));
+  TRY32(sort_step(h, true));
   const C32 c = make_c32(h, 0, 0.5, 1. / 6.);
   if (h->np > 0) {
     k_prime32<<<nb(h->np), kThreads, 0, h->stream>>>(h->geom, f, c.itth, h->np);
