@@ -185,7 +185,7 @@ int refresh_ghosts(pstep_ctx *h, double *f);
 int interior_mean(pstep_ctx *h, const double *f, double *out_dev);
 int momentum_sums(pstep_ctx *h);
 int f32_download(pstep_ctx *h, double *const dst[7], int32_t *flag, int on_device);
-const double *f32_field_stats_dev(pstep_ctx *h, int field);
+int f32_field_stats(pstep_ctx *h, int field, double r[3]);
 int f32_fused_max(pstep_ctx *h, int id, double *out);
 int f64_fused_max(pstep_ctx *h, int id, double *out);
 int order_passes(pstep_ctx *h);

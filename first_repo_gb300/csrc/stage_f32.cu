@@ -114,6 +114,7 @@ struct F32Form {
   int32_t *se;        // fixed-point scale exponents per field
   unsigned long long *totals;  // exact integer sums, maxima, minima of the five fields (last deposit)
   double *fstat;               // per field: max, min, interior sum as fp64 (k_totals)
+  int ext_ok[5];               // per field: its last deposit gathered the extrema too
   Work work;
   int launch_no;      // deposit launches since the last work-list build (counter index)
   void *corr_mem;     // learned correction: packed weight image + biases (device), or nullptr
@@ -1118,7 +1119,7 @@ template <bool DO_INT, bool DO_NEW, int BR, int BZ>
 __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
     k_dep32(Geom G, F32Form f, Set32 SI, Set32 SN, Work w, int twc, double *__restrict__ outC,
             double *__restrict__ outX, double *__restrict__ outY, double *__restrict__ outZ,
-            double *__restrict__ outE, unsigned long long *__restrict__ totals) {
+            double *__restrict__ outE, unsigned long long *__restrict__ totals, int ext) {
   constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
   constexpr int FE = DO_INT ? 4 : 0;  // accumulator index of RHS_Part_Temp
   constexpr int NB = BR * BR * BZ;
@@ -1287,8 +1288,10 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
         if (zero_ru) v = 0;
         out[g] = fixed_to_f64(v, se[fld]);
         tot[fld] += v;
-        vmax[fld] = max(vmax[fld], v);
-        vmin[fld] = min(vmin[fld], v);
+        if (ext) {
+          vmax[fld] = max(vmax[fld], v);
+          vmin[fld] = min(vmin[fld], v);
+        }
       }
     }
     {
@@ -1297,11 +1300,13 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
       for (int fld = 0; fld < 5; ++fld) {
         if (fld < 4 ? !DO_INT : !DO_NEW) continue;
         const long long sm = warp_sum_i64(tot[fld]);
-        const long long mx = warp_max_i64(vmax[fld]), mn = warp_min_i64(vmin[fld]);
-        if (lane == 0) {
-          wsum[wid * 5 + fld] += sm;
-          wmax[wid * 5 + fld] = max(wmax[wid * 5 + fld], mx);
-          wmin[wid * 5 + fld] = min(wmin[wid * 5 + fld], mn);
+        if (lane == 0) wsum[wid * 5 + fld] += sm;
+        if (ext) {  // the same for every thread of the launch
+          const long long mx = warp_max_i64(vmax[fld]), mn = warp_min_i64(vmin[fld]);
+          if (lane == 0) {
+            wmax[wid * 5 + fld] = max(wmax[wid * 5 + fld], mx);
+            wmin[wid * 5 + fld] = min(wmin[wid * 5 + fld], mn);
+          }
         }
       }
     }
@@ -1321,8 +1326,10 @@ __global__ void __launch_bounds__(DepTraits<BR, BZ>::kThreads)
         mn = min(mn, wmin[w2 * 5 + fld]);
       }
       if (r) atomicAdd(&totals[fld], (unsigned long long)r);
-      atomicMax(reinterpret_cast<long long *>(&totals[5 + fld]), mx);
-      atomicMin(reinterpret_cast<long long *>(&totals[10 + fld]), mn);
+      if (ext) {
+        atomicMax(reinterpret_cast<long long *>(&totals[5 + fld]), mx);
+        atomicMin(reinterpret_cast<long long *>(&totals[10 + fld]), mn);
+      }
     }
   }
 }
@@ -1339,14 +1346,16 @@ __global__ void k_dep_stats_init(unsigned long long *__restrict__ totals, int do
 // words as fp64 (correctly rounded): the momentum components' sums, the interior mean
 // of RHS_Part_Temp (grid.cpp:541), and per field max, min and interior sum
 // (fstat[3 q .. 3 q + 2]) for the fields this launch wrote.
-__global__ void k_totals(F32Form f, const unsigned long long *__restrict__ totals, int do_int, int do_new,
+__global__ void k_totals(F32Form f, const unsigned long long *__restrict__ totals, int do_int, int do_new, int ext,
                          double inv_cells, double *__restrict__ mom, double *__restrict__ emean,
                          double *__restrict__ fstat) {
   const int q = threadIdx.x;
   if (q >= 5 || !(q < 4 ? do_int : do_new)) return;
   const int se = f.se[q];
-  fstat[3 * q + 0] = fixed_to_f64((long long)totals[5 + q], se);
-  fstat[3 * q + 1] = fixed_to_f64((long long)totals[10 + q], se);
+  if (ext) {
+    fstat[3 * q + 0] = fixed_to_f64((long long)totals[5 + q], se);
+    fstat[3 * q + 1] = fixed_to_f64((long long)totals[10 + q], se);
+  }
   fstat[3 * q + 2] = fixed_to_f64((long long)totals[q], se);
   if (q >= 1 && q <= 3) mom[q - 1] = fstat[3 * q + 2];
   if (q == 4) *emean = fstat[3 * q + 2] * inv_cells;
@@ -1510,7 +1519,7 @@ void dfree32(T *&p) {
     if (rc_ != PSTEP_OK) return rc_;   \
   } while (0)
 
-int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN);
+int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN, bool ext);
 
 // check_sorted: first test whether the storage is in key order already (a population
 // uploaded as an earlier step left it, e.g. a host round trip), and then only build the
@@ -1987,7 +1996,7 @@ int f32_prime(pstep_ctx *h) {
     PSTEP_LAUNCHED(h);
   }
   // part2gas_Temp_int at the base positions
-  return dep_launch(h, false, true, f.set[SBASE], f.set[SBASE]);
+  return dep_launch(h, false, true, f.set[SBASE], f.set[SBASE], true);
 }
 
 int f32_stage(pstep_ctx *h, int k, double pre, double post) {
@@ -2035,9 +2044,11 @@ int f32_stage(pstep_ctx *h, int k, double pre, double post) {
     PSTEP_LAUNCHED(h);
   }
   prof_end(h, PSTEP_PHASE_ADVANCE);
-  // one walk: concentration + momentum at *_int (the base itself at stage 0), RHS_T at *_new
+  // one walk: concentration + momentum at *_int (the base itself at stage 0), RHS_T at *_new;
+  // the field extrema (pstep_field_stats) only in the step's last stage, whose fields the
+  // step leaves
   prof_begin(h, PSTEP_PHASE_DEPOSIT_INT);
-  TRY32(dep_launch(h, true, true, f.set[h->int_is_base ? SBASE : SINT], f.set[SNEW]));
+  TRY32(dep_launch(h, true, true, f.set[h->int_is_base ? SBASE : SINT], f.set[SNEW], k == 3));
   prof_end(h, PSTEP_PHASE_DEPOSIT_INT);
   return PSTEP_OK;
 }
@@ -2046,7 +2057,7 @@ namespace {
 // one launch of the deposit variant for (do_int, do_new) with bricks BR x BR x BZ:
 // persistent CTAs (as many as fit on the SMs) pulling work items
 template <bool DO_INT, bool DO_NEW, int BR, int BZ>
-int dep_run1(pstep_ctx *h, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z, double *E) {
+int dep_run1(pstep_ctx *h, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z, double *E, int ext) {
   constexpr int NF = (DO_INT ? 4 : 0) + (DO_NEW ? 1 : 0);
   constexpr size_t smem = DepSmem<BR, BZ, NF>::kBytes;
   auto kern = k_dep32<DO_INT, DO_NEW, BR, BZ>;
@@ -2059,20 +2070,20 @@ int dep_run1(pstep_ctx *h, Set32 SI, Set32 SN, double *C, double *X, double *Y, 
   }
   F32Form &f = *h->f32;
   kern<<<h->num_sms * per_sm, DepTraits<BR, BZ>::kThreads, smem, h->stream>>>(h->geom, f, SI, SN, f.work,
-                                                                               h->cfg.twc, C, X, Y, Z, E, f.totals);
+                                                                               h->cfg.twc, C, X, Y, Z, E, f.totals, ext);
   PSTEP_LAUNCHED(h);
   return PSTEP_OK;
 }
 
 template <int BR, int BZ>
 int dep_run(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN, double *C, double *X, double *Y, double *Z,
-            double *E) {
-  if (do_int && do_new) return dep_run1<true, true, BR, BZ>(h, SI, SN, C, X, Y, Z, E);
-  if (do_int) return dep_run1<true, false, BR, BZ>(h, SI, SN, C, X, Y, Z, E);
-  return dep_run1<false, true, BR, BZ>(h, SI, SN, C, X, Y, Z, E);
+            double *E, int ext) {
+  if (do_int && do_new) return dep_run1<true, true, BR, BZ>(h, SI, SN, C, X, Y, Z, E, ext);
+  if (do_int) return dep_run1<true, false, BR, BZ>(h, SI, SN, C, X, Y, Z, E, ext);
+  return dep_run1<false, true, BR, BZ>(h, SI, SN, C, X, Y, Z, E, ext);
 }
 
-int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
+int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN, bool ext) {
   F32Form &f = *h->f32;
   k_scales<<<1, 32, 0, h->stream>>>(f);  // fold this advance's maxima into the fixed-point scales
   PSTEP_LAUNCHED(h);
@@ -2082,10 +2093,12 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   double *C = h->dep[PSTEP_FIELD_C], *X = h->dep[PSTEP_FIELD_RU_X], *Y = h->dep[PSTEP_FIELD_RU_Y],
          *Z = h->dep[PSTEP_FIELD_RU_Z], *E = h->dep[PSTEP_FIELD_PART_TEMP];
   if (f.work.br == 16) {
-    TRY32((dep_run<16, 16>(h, do_int, do_new, SI, SN, C, X, Y, Z, E)));
+    TRY32((dep_run<16, 16>(h, do_int, do_new, SI, SN, C, X, Y, Z, E, ext ? 1 : 0)));
   } else {
-    TRY32((dep_run<8, 8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E)));
+    TRY32((dep_run<8, 8>(h, do_int, do_new, SI, SN, C, X, Y, Z, E, ext ? 1 : 0)));
   }
+  for (int q = 0; q < 5; ++q)
+    if (q < 4 ? do_int : do_new) f.ext_ok[q] = ext ? 1 : 0;
   // interior values are final (periodic targets): refresh the ghost layers only
   if (do_int) {
     double *all[4] = {C, X, Y, Z};
@@ -2098,7 +2111,7 @@ int dep_launch(pstep_ctx *h, bool do_int, bool do_new, Set32 SI, Set32 SN) {
   // balance sums from the deposit's exact integer totals: the momentum components and
   // the interior mean of RHS_Part_Temp (grid.cpp:541)
   const Geom &G = h->geom;
-  k_totals<<<1, 32, 0, h->stream>>>(f, f.totals, do_int ? 1 : 0, do_new ? 1 : 0,
+  k_totals<<<1, 32, 0, h->stream>>>(f, f.totals, do_int ? 1 : 0, do_new ? 1 : 0, ext ? 1 : 0,
                                     1.0 / ((double)G.n[0] * G.n[1] * G.n[2]), h->mom_dev, h->emean_dev, f.fstat);
   PSTEP_LAUNCHED(h);
   return PSTEP_OK;
@@ -2125,9 +2138,16 @@ int f32_fused_max(pstep_ctx *h, int id, double *out) {
   return PSTEP_OK;
 }
 
-// device address of a deposited field's max, min and interior sum of the last deposit
-// that wrote it (FP32 form)
-const double *f32_field_stats_dev(pstep_ctx *h, int field) { return h->f32->fstat + 3 * field; }
+// a deposited field's max, min and interior sum as the last deposit that wrote it
+// gathered them (FP32 form): PSTEP_OK with r set, or -1 when that deposit did not gather
+// the extrema (a stage other than a step's last; the caller then makes a pass)
+int f32_field_stats(pstep_ctx *h, int field, double r[3]) {
+  F32Form &f = *h->f32;
+  if (!f.ext_ok[field]) return -1;
+  PSTEP_CUDA(cudaMemcpyAsync(r, f.fstat + 3 * field, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  PSTEP_CUDA(cudaStreamSynchronize(h->stream));
+  return PSTEP_OK;
+}
 
 int f32_end_stage(pstep_ctx *h) {
   F32Form &f = *h->f32;

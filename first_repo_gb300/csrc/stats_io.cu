@@ -200,15 +200,17 @@ int pstep_field_stats(pstep_handle h, int field, double *max, double *min, doubl
   if (!h || field < 0 || field >= PSTEP_NUM_FIELDS) return PSTEP_ERR_ARG;
   const Geom &G = h->geom;
   if (h->f32) {
-    // the FP32 form's deposit gathers these in its flush (exact integer max, min, sum)
+    // the FP32 form's last-stage deposit gathers these in its flush (exact integer max,
+    // min, sum); after any other deposit a pass below
     double r[3] = {0, 0, 0};
-    cudaError_t e = cudaMemcpyAsync(r, f32_field_stats_dev(h, field), sizeof r, cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) return fail_io(h, PSTEP_ERR_CUDA, std::string("field stats: ") + cudaGetErrorString(e));
-    if (max) *max = r[0];
-    if (min) *min = r[1];
-    if (mean) *mean = r[2] / (double)((long long)G.n[0] * G.n[1] * G.n[2]);
-    return PSTEP_OK;
+    const int fr = f32_field_stats(h, field, r);
+    if (fr == PSTEP_OK) {
+      if (max) *max = r[0];
+      if (min) *min = r[1];
+      if (mean) *mean = r[2] / (double)((long long)G.n[0] * G.n[1] * G.n[2]);
+      return PSTEP_OK;
+    }
+    if (fr != -1) return fr;
   }
   double *part = nullptr;
   int rc = dalloc_tmp(h, part, 3 * kStatBlocks + 3);

@@ -103,7 +103,10 @@ def test_fp32_snapshot_round_trip_and_statistics(built_cuda, tmp_path):
     assert g.np_tot() == COUNT
     for k in KEYS:
         assert g.max(k) == pyoracle.array_max(got[k]), k
+    # after the step, the extrema come from its last deposit (no kernel launch) ...
+    before = g.launches()
     _check_field_stats(g)
+    assert g.launches() == before
     tags = [0, 11, COUNT - 1, -5, 11]  # an absent id and a repeated one
     xyz, found = g.find_tags(tags)
     where = {int(f): i for i, f in enumerate(got["flag"])}
@@ -125,6 +128,11 @@ def test_fp32_snapshot_round_trip_and_statistics(built_cuda, tmp_path):
     with pytest.raises(pstep.PstepError) as e:
         g2.load_all(d, COUNT, box=False)  # no _IO files
     assert e.value.status == 11
+    # ... after a stage that is not a step's last, from a pass over the fields
+    g.stage(0)
+    before = g.launches()
+    _check_field_stats(g)
+    assert g.launches() > before
     g.close()
     g2.close()
 
