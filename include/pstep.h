@@ -325,10 +325,11 @@ int pstep_balance_index(pstep_handle h, double *out);
 /* tensor0::max, ::min and ::mean (tensor0.cpp:452-463, 492-503, 418-435) of a deposited
  * field (PSTEP_FIELD_*), over the interior cells. The maximum and minimum are exact; the
  * mean is the interior sum (taken in a fixed order, not the reference's i-j-k loop
- * order, so it can differ in the last bits) over n^3. PSTEP_FP32: gathered by the deposit
- * itself as it writes the field (exact integer maximum, minimum and sum, the sum rounded
- * once), so the call reads three numbers and makes no pass over the grid. Any of the
- * outputs may be NULL. */
+ * order, so it can differ in the last bits) over n^3. PSTEP_FP32, after pstep_end_step
+ * (or pstep_run) or pstep_prime: gathered by the last deposit as it wrote the field
+ * (exact integer maximum, minimum and sum, the sum rounded once), so the call reads three
+ * numbers and makes no pass over the grid; after a stage other than a step's last, a
+ * pass. Any of the outputs may be NULL. */
 int pstep_field_stats(pstep_handle h, int field, double *max, double *min, double *mean);
 /* particle::find_tag (particle.cpp:721-731) for n ids: xyz[3 i .. 3 i + 2] = the position of
  * the particle with id tags[i] and found[i] = 1, or found[i] = 0 (xyz untouched) when no
